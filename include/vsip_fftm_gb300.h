@@ -258,17 +258,25 @@ int jvsip_fftm_batch_f(size_t n, const vsip_fftm_f *const plans[],
 /* A captured batch: the descriptor queue is built and uploaded once and the
  * launch is recorded in a CUDA graph; jvsip_fftm_batch_run_f replays it.
  * The views' blocks must stay admitted (device addresses are baked in). */
-typedef struct jvsip_fftm_batch_s jvsip_fftm_batch_f;
-jvsip_fftm_batch_f *jvsip_fftm_batch_create_f(size_t n, const vsip_fftm_f *const plans[],
+typedef struct jvsip_fftm_batchplan_s jvsip_fftm_batchplan_f;
+jvsip_fftm_batchplan_f *jvsip_fftm_batch_create_f(size_t n, const vsip_fftm_f *const plans[],
                                               const vsip_cmview_f *const in[],
                                               const vsip_cmview_f *const out[]);
-int  jvsip_fftm_batch_run_f(jvsip_fftm_batch_f *batch);
-int  jvsip_fftm_batch_destroy_f(jvsip_fftm_batch_f *batch);
+int  jvsip_fftm_batch_run_f(jvsip_fftm_batchplan_f *batch);
+int  jvsip_fftm_batch_destroy_f(jvsip_fftm_batchplan_f *batch);
 
 /* Library / device information for tools (kernels compiled, SM count). */
 const char *jvsip_gpu_build_info(void);
 /* Device-side synchronisation: returns when all work this library queued has finished. */
 int jvsip_gpu_synchronize(void);
+/* The CUDA stream (cudaStream_t, as void*) all of this library's device work
+ * is ordered on; callers may record events on it or make their streams wait. */
+void *jvsip_gpu_stream(void);
+/* Plan introspection: the device pass radices (returns their count) and the
+ * reference's digit-reversal map of the plan length (c_VSIP_src/VI_jofk.h),
+ * kept for parity checks (returns the map length). */
+int  jvsip_fftm_passes(const void *plan, int *radix, int cap);
+long jvsip_fftm_jofk(const void *plan, unsigned long *out, long cap);
 
 #ifdef __cplusplus
 }

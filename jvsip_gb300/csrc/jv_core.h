@@ -1,0 +1,139 @@
+// jv_core.h -- internal interfaces of the GB300 fftm library: error state,
+// device context, device memory pool, block residency table, plan object and
+// the kernel launch descriptors shared by the host runtime and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "vsip_layout.h"
+
+namespace jv {
+
+// ------------------------------------------------------------------ errors
+// Error codes returned by jvsip_gpu_last_error().
+enum Err {
+    OK = 0,
+    E_NODEVICE = 1,    // no usable CUDA device
+    E_ALLOC = 2,       // device or pinned allocation failed
+    E_ARG = 3,         // invalid plan / view / length
+    E_CUDA = 4,        // a CUDA runtime call failed
+    E_UNSUPPORTED = 5, // combination this library does not handle
+    E_DEVICE = 6       // a kernel reported a device-side status (bounded wait expired)
+};
+void set_error(int code, const std::string &msg);
+bool cuda_ok(cudaError_t e, const char *what);   // records and returns false on error
+
+// ------------------------------------------------------------------ device
+struct Device {
+    int id = -1;
+    int sms = 0;
+    size_t smem_optin = 0;     // max dynamic shared memory per block (opt-in)
+    cudaStream_t stream = nullptr;  // library stream (all device work is ordered on it)
+    cudaStream_t h2d = nullptr;     // staging copy streams for host-resident views
+    cudaStream_t d2h = nullptr;
+};
+Device *device();   // lazily initialised; nullptr (and error recorded) when no GPU
+
+// ------------------------------------------------------------------ memory pool
+// Caching device allocator: freed buffers are kept per exact size class and
+// reused, so repeated calls do not cudaMalloc.  Thread-safe.
+void *dmalloc(size_t bytes);
+void dfree(void *p);
+void pool_trim();
+
+// ------------------------------------------------------------------ residency
+// Device mirror of an admitted block.  For interleaved complex blocks `d` holds
+// 2*size scalars; for split blocks `d` holds the real part and `d_im` the
+// imaginary part; for real blocks `d` holds size*rstride scalars.
+struct Mirror {
+    void *d = nullptr;
+    void *d_im = nullptr;
+    size_t bytes = 0;          // bytes of each device array
+    bool device_newer = false; // device written since the last host sync
+};
+Mirror *mirror_find(const void *block);           // nullptr when the block is not mirrored
+Mirror *mirror_create(const void *block, size_t bytes, bool split);
+void mirror_drop(const void *block);
+
+// Pinned host arrays handed out by vsip_*blockcreate_* (freed with cudaFreeHost).
+bool pinned_owned(const void *p);
+void *host_alloc(size_t bytes);
+void host_free(void *p);
+
+// ------------------------------------------------------------------ views on the device
+// A complex view in transform order: element n of vector v is at complex index
+// off + v*vs + n*es of the arrays (re, im); scalar index = cst * complex index.
+struct CView {
+    void *re = nullptr, *im = nullptr;
+    long cst = 2, off = 0, es = 1, vs = 0;
+};
+// A real view in transform order: element n of vector v at a[rst*(off + v*vs + n*es)].
+struct RView {
+    void *a = nullptr;
+    long rst = 1, off = 0, es = 1, vs = 0;
+};
+
+enum Kind { K_C2C = 0, K_R2C = 1, K_C2R = 2 };
+enum Prec { P_F32 = 0, P_F64 = 1 };
+
+// One execution of a plan on resolved device views.
+struct Job {
+    int kind = K_C2C;
+    int prec = P_F32;
+    long N = 0;          // complex FFT length (R2C/C2R: the half length MN)
+    long nvec = 0;       // number of transforms
+    int inv = 0;         // 1: inverse direction (exp(+2 pi i nk/N))
+    int has_scale = 0;
+    double scale = 1.0;
+    CView cin, cout;     // complex input / output
+    RView rin, rout;     // real input (R2C) / output (C2R)
+    int inplace = 0;     // input and output are the same storage
+    const void *tw = nullptr;     // forward table exp(-2 pi i m/N), m < N, dtype complex
+    const void *thalf = nullptr;  // R2C/C2R table exp(-+ i pi k/MN), k <= MN
+    int npass = 0;
+    int radix[40];
+};
+
+// Kernel entry points (defined in the kernel translation units).
+bool launch_smem_f32(const Job &j, cudaStream_t s);
+bool launch_smem_f64(const Job &j, cudaStream_t s);
+bool launch_global_f32(const Job &j, cudaStream_t s);
+bool launch_global_f64(const Job &j, cudaStream_t s);
+bool launch_fast_f32(const Job &j, cudaStream_t s);   // specialised kernels; false when none fits
+
+// Capacity queries used by the dispatcher.
+long smem_max_len(int prec, int kind);   // largest N the shared-memory kernel takes
+
+// ------------------------------------------------------------------ plans
+struct Plan {
+    int type = JV_CCFFTOP;    // JV_CCFFTOP / CCFFTIP / RCFFTOP / CRFFTOP
+    int prec = P_F32;
+    long M = 0, N = 0, MN = 0, mN = 0;
+    int major = 0;            // 0 = VSIP_ROW, 1 = VSIP_COL
+    int dir = -1;
+    double scale = 1.0;
+    unsigned ntimes = 0;
+    int hint = 0;
+    int form = 0;             // JVSIP_FORM_*
+    std::vector<int> radix;   // pass radices of the device kernels (product = MN)
+    bool smooth = true;       // every radix is one of the built-in codelets
+    void *d_tw = nullptr;     // forward twiddles, MN entries
+    void *d_thalf = nullptr;  // half-angle table, MN+1 entries (real transforms)
+    std::vector<unsigned long> jofk;  // reference digit-reversal map (kept for parity checks)
+    std::mutex mu;            // the plan is used by one call at a time
+};
+
+Plan *plan_of(const void *vsip_plan);   // ext_fftm_obj of a vsip_fftm_* (nullptr if bad)
+
+// factorisation of the reference (c_VSIP_src/VI_nuV.h:22-136); returns the stage count
+unsigned long ref_factor(unsigned long N, unsigned long *pn, unsigned long *p0, unsigned long *pF);
+// device pass radices for length N: codelets 16, 8, 4, 2, 5, 3, 7, then any other prime
+std::vector<int> pass_radices(long N, bool *smooth);
+
+}  // namespace jv

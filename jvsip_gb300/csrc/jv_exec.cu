@@ -1,0 +1,469 @@
+// jv_exec.cu -- vsip_ccfftmop/ccfftmip/rcfftmop/crfftmop in _f and _d.
+//
+// Semantics follow the reference (c_VSIP_src/VI_ccfftmop_f_def.h:20-29,
+// VI_ccfftmip_f_def.h:17-23, VI_rcfftmop_f_def.h:24-120,
+// VI_crfftmop_f_def.h:25-126): plan.mN transforms of length plan.MN along the
+// rows (VSIP_ROW) or columns (VSIP_COL) of the views, y = scale * DFT_dir(x),
+// the scale applied only when it is not 1, any signed strides and offsets,
+// interleaved or split complex blocks, and x may alias y.
+//
+// Each view is resolved to device memory: a block admitted through this
+// library is used in place in its device mirror; any other block is staged --
+// the span of the block the view touches is copied to the device before the
+// kernels and (for outputs) back after them, inside the call.
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "jv_core.h"
+
+namespace jv {
+
+long smem_max_len_f32(int kind);
+long smem_max_len_f64(int kind);
+
+long smem_max_len(int prec, int kind) { return prec == P_F32 ? smem_max_len_f32(kind) : smem_max_len_f64(kind); }
+
+// ---------------------------------------------------------------- staging of host blocks
+// One staged region: scalars [lo*cst, (hi+1)*cst) of a host array (and of its
+// imaginary array for split blocks) copied to one device buffer.
+struct Region {
+    const void *key = nullptr;   // block identity
+    char *h_re = nullptr, *h_im = nullptr;
+    size_t esz = 0;              // bytes per scalar
+    long cst = 1;                // scalars per element index step
+    long lo = 0, hi = -1;        // element index range
+    bool read = false, write = false;
+    void *d_re = nullptr, *d_im = nullptr;
+};
+
+struct Staging {
+    std::vector<Region> regs;
+    Region *find(const void *key) {
+        for (auto &r : regs)
+            if (r.key == key) return &r;
+        return nullptr;
+    }
+    void add(const void *key, char *h_re, char *h_im, size_t esz, long cst, long lo, long hi, bool rd, bool wr) {
+        Region *r = find(key);
+        if (r) {
+            r->lo = std::min(r->lo, lo);
+            r->hi = std::max(r->hi, hi);
+            r->read = r->read || rd;
+            r->write = r->write || wr;
+            return;
+        }
+        Region n;
+        n.key = key;
+        n.h_re = h_re;
+        n.h_im = h_im;
+        n.esz = esz;
+        n.cst = cst;
+        n.lo = lo;
+        n.hi = hi;
+        n.read = rd;
+        n.write = wr;
+        regs.push_back(n);
+    }
+    size_t bytes(const Region &r) const { return (size_t)(r.hi - r.lo + 1) * r.cst * r.esz; }
+    bool upload(cudaStream_t st) {
+        for (auto &r : regs) {
+            size_t b = bytes(r);
+            r.d_re = dmalloc(b);
+            if (!r.d_re) return false;
+            if (r.h_im) {
+                r.d_im = dmalloc(b);
+                if (!r.d_im) return false;
+            }
+            if (r.read) {
+                size_t o = (size_t)r.lo * r.cst * r.esz;
+                if (!cuda_ok(cudaMemcpyAsync(r.d_re, r.h_re + o, b, cudaMemcpyHostToDevice, st), "stage in"))
+                    return false;
+                if (r.h_im && !cuda_ok(cudaMemcpyAsync(r.d_im, r.h_im + o, b, cudaMemcpyHostToDevice, st), "stage in"))
+                    return false;
+            }
+        }
+        return true;
+    }
+    bool download(cudaStream_t st) {
+        bool ok = true;
+        for (auto &r : regs) {
+            if (!r.write || !r.d_re) continue;
+            size_t b = bytes(r), o = (size_t)r.lo * r.cst * r.esz;
+            ok = ok && cuda_ok(cudaMemcpyAsync(r.h_re + o, r.d_re, b, cudaMemcpyDeviceToHost, st), "stage out");
+            if (r.h_im) ok = ok && cuda_ok(cudaMemcpyAsync(r.h_im + o, r.d_im, b, cudaMemcpyDeviceToHost, st), "stage out");
+        }
+        return ok;
+    }
+    ~Staging() {
+        for (auto &r : regs) {
+            dfree(r.d_re);
+            dfree(r.d_im);
+        }
+    }
+};
+
+// ---------------------------------------------------------------- view geometry
+struct Geo {
+    long off, es, vs, len, nvec;
+    long lo() const { return off + std::min(0L, (nvec - 1) * vs) + std::min(0L, (len - 1) * es); }
+    long hi() const { return off + std::max(0L, (nvec - 1) * vs) + std::max(0L, (len - 1) * es); }
+    // covers its span exactly once (no gaps), so an output needs no copy-in
+    bool dense() const {
+        long span = hi() - lo() + 1;
+        if (span != len * nvec) return false;
+        return (labs(es) == 1 && (nvec == 1 || labs(vs) == len)) || (labs(vs) == 1 && (len == 1 || labs(es) == nvec));
+    }
+};
+
+template <typename CMV>
+static Geo cgeo(const CMV *v, int major, long len, long nvec) {
+    Geo g;
+    g.off = (long)v->offset;
+    if (major == 0) {
+        g.es = v->row_stride;
+        g.vs = v->col_stride;
+    } else {
+        g.es = v->col_stride;
+        g.vs = v->row_stride;
+    }
+    g.len = len;
+    g.nvec = nvec;
+    return g;
+}
+
+template <typename CMV>
+static bool view_ok(const CMV *v, int major, long len, long nvec) {
+    if (!v || !v->block) return false;
+    long vl = (long)(major == 0 ? v->row_length : v->col_length);
+    long vn = (long)(major == 0 ? v->col_length : v->row_length);
+    return vl >= len && vn >= nvec;
+}
+
+// Resolve a complex view: device mirror in place, or a staged region.
+template <typename T, typename CB>
+struct CRes {
+    const CB *blk;
+    Geo g;
+    Mirror *m;
+};
+
+template <typename T, typename CB>
+static void stage_c(Staging &s, const CRes<T, CB> &r, bool rd, bool wr) {
+    if (r.m) return;
+    const CB *b = r.blk;
+    bool split = (b->cstride == 1);
+    char *h_re = (char *)b->R->array;
+    char *h_im = split ? (char *)b->I->array : nullptr;
+    s.add(b, h_re, h_im, sizeof(T), split ? 1 : 2, r.g.lo(), r.g.hi(), rd, wr);
+}
+
+template <typename T, typename CB>
+static CView dev_c(Staging &s, const CRes<T, CB> &r) {
+    CView v;
+    v.es = r.g.es;
+    v.vs = r.g.vs;
+    bool split = (r.blk->cstride == 1);
+    v.cst = split ? 1 : 2;
+    if (r.m) {
+        v.re = r.m->d;
+        v.im = split ? r.m->d_im : (void *)((T *)r.m->d + 1);
+        v.off = r.g.off;
+    } else {
+        Region *g = s.find(r.blk);
+        v.re = g->d_re;
+        v.im = split ? g->d_im : (void *)((T *)g->d_re + 1);
+        v.off = r.g.off - g->lo;
+    }
+    return v;
+}
+
+// Real views: the block may be a user/VSIPL real block or the real/imaginary
+// part of a complex block (its parent).
+template <typename T, typename RB>
+struct RRes {
+    const RB *blk;
+    Geo g;
+    void *dbase;  // device address of the block's array (mirrored), else nullptr
+    long rst;
+};
+
+template <typename T, typename RB>
+static RRes<T, RB> resolve_r(const RB *b, const Geo &g) {
+    RRes<T, RB> r;
+    r.blk = b;
+    r.g = g;
+    r.dbase = nullptr;
+    r.rst = b->rstride > 0 ? b->rstride : 1;
+    Mirror *m = mirror_find(b);
+    if (m) {
+        r.dbase = m->d;
+    } else if (b->parent) {
+        Mirror *pm = mirror_find(b->parent);
+        if (pm) {
+            bool split = (b->parent->cstride == 1);
+            if (b == b->parent->R) r.dbase = pm->d;
+            else r.dbase = split ? pm->d_im : (void *)((T *)pm->d + 1);
+        }
+    }
+    return r;
+}
+
+template <typename T, typename RB>
+static void stage_r(Staging &s, const RRes<T, RB> &r, bool rd, bool wr) {
+    if (r.dbase) return;
+    s.add(r.blk, (char *)r.blk->array, nullptr, sizeof(T), r.rst, r.g.lo(), r.g.hi(), rd, wr);
+}
+
+template <typename T, typename RB>
+static RView dev_r(Staging &s, const RRes<T, RB> &r) {
+    RView v;
+    v.rst = r.rst;
+    v.es = r.g.es;
+    v.vs = r.g.vs;
+    if (r.dbase) {
+        v.a = r.dbase;
+        v.off = r.g.off;
+    } else {
+        Region *g = s.find(r.blk);
+        v.a = g->d_re;
+        v.off = r.g.off - g->lo;
+    }
+    return v;
+}
+
+static void mark_written(const void *blk) {
+    Mirror *m = mirror_find(blk);
+    if (m) m->device_newer = true;
+}
+
+// ---------------------------------------------------------------- dispatch
+static bool run_job(Job &j, cudaStream_t st) {
+    if (j.nvec <= 0 || j.N <= 0) return true;
+    long lim = smem_max_len(j.prec, j.kind);
+    bool smooth = true;
+    for (int i = 0; i < j.npass; i++)
+        if (j.radix[i] != 2 && j.radix[i] != 3 && j.radix[i] != 4 && j.radix[i] != 5 && j.radix[i] != 7 &&
+            j.radix[i] != 8)
+            smooth = false;
+    long need = j.N + (j.kind == K_C2R ? 1 : 0);
+    if (smooth && need <= lim) {
+        if (j.prec == P_F32) {
+            if (launch_fast_f32(j, st)) return true;
+            return launch_smem_f32(j, st);
+        }
+        return launch_smem_f64(j, st);
+    }
+    return j.prec == P_F32 ? launch_global_f32(j, st) : launch_global_f64(j, st);
+}
+
+// Staged (host) views: copy results back and wait, so the host data is
+// current when the call returns.  All-resident calls return asynchronously;
+// work on the library stream is ordered, and release / sync wait for it.
+static bool finish(Staging &stg, cudaStream_t st, bool ok) {
+    if (stg.regs.empty()) return ok;
+    ok = ok && stg.download(st);
+    return cuda_ok(cudaStreamSynchronize(st), "fftm execution") && ok;
+}
+
+static void fill_job(Job &j, const Plan *p, int kind) {
+    j.kind = kind;
+    j.prec = p->prec;
+    j.N = p->MN;
+    j.nvec = p->mN;
+    j.inv = (p->dir == 1) ? 1 : 0;
+    j.has_scale = (p->scale != 1.0) ? 1 : 0;
+    j.scale = p->scale;
+    j.tw = p->d_tw;
+    j.thalf = p->d_thalf;
+    j.npass = (int)p->radix.size();
+    for (int i = 0; i < j.npass && i < 40; i++) j.radix[i] = p->radix[i];
+}
+
+template <typename T, typename VP, typename CMV, typename CB>
+static void exec_cc(const VP *vp, const CMV *x, const CMV *y, bool ip) {
+    Plan *p = plan_of(vp);
+    if (!p) {
+        set_error(E_ARG, "invalid fftm plan");
+        return;
+    }
+    if (p->type != JV_CCFFTOP && p->type != JV_CCFFTIP) {
+        set_error(E_ARG, "plan is not a complex-to-complex plan");
+        return;
+    }
+    Device *d = device();
+    if (!d) return;
+    std::lock_guard<std::mutex> lk(p->mu);
+    if (!view_ok(x, p->major, p->MN, p->mN) || (!ip && !view_ok(y, p->major, p->MN, p->mN))) {
+        set_error(E_ARG, "view smaller than the plan");
+        return;
+    }
+    Job j;
+    fill_job(j, p, K_C2C);
+    CRes<T, CB> rx{x->block, cgeo(x, p->major, p->MN, p->mN), mirror_find(x->block)};
+    CRes<T, CB> ry = rx;
+    bool same_view = ip;
+    if (!ip) {
+        ry = CRes<T, CB>{y->block, cgeo(y, p->major, p->MN, p->mN), mirror_find(y->block)};
+        same_view = (x->block == y->block && rx.g.off == ry.g.off && rx.g.es == ry.g.es && rx.g.vs == ry.g.vs);
+    }
+    Staging stg;
+    cudaStream_t st = d->stream;
+    stage_c(stg, rx, true, same_view);
+    if (!same_view) stage_c(stg, ry, !ry.g.dense() || (y->block == x->block), true);
+    if (!stg.upload(st)) return;
+    j.cin = dev_c(stg, rx);
+    j.cout = same_view ? j.cin : dev_c(stg, ry);
+    j.inplace = same_view ? 1 : 0;
+    void *tmp = nullptr;
+    if (!same_view && x->block == y->block) {
+        long xl = rx.g.lo(), xh = rx.g.hi(), yl = ry.g.lo(), yh = ry.g.hi();
+        if (!(xh < yl || yh < xl)) {
+            // x and y overlap in one block: transform from a private copy of x
+            // (the reference copies x into y first, VI_ccfftmop_f_def.h:26)
+            size_t n = (size_t)(xh - xl + 1);
+            bool split = (x->block->cstride == 1);
+            size_t b = n * (split ? 1 : 2) * sizeof(T);
+            tmp = dmalloc(split ? 2 * b : b);
+            if (!tmp) return;
+            Geo gd = rx.g;
+            gd.off = j.cin.off;  // x's geometry in device index space
+            xl = gd.lo();
+            char *src_re = (char *)j.cin.re + (size_t)xl * j.cin.cst * sizeof(T);
+            if (!split) {
+                if (!cuda_ok(cudaMemcpyAsync(tmp, src_re, b, cudaMemcpyDeviceToDevice, st), "alias copy")) return;
+                j.cin.re = tmp;
+                j.cin.im = (T *)tmp + 1;
+            } else {
+                char *src_im = (char *)j.cin.im + (size_t)xl * sizeof(T);
+                if (!cuda_ok(cudaMemcpyAsync(tmp, src_re, b, cudaMemcpyDeviceToDevice, st), "alias copy") ||
+                    !cuda_ok(cudaMemcpyAsync((char *)tmp + b, src_im, b, cudaMemcpyDeviceToDevice, st), "alias copy"))
+                    return;
+                j.cin.re = tmp;
+                j.cin.im = (char *)tmp + b;
+            }
+            j.cin.off -= xl;
+        }
+    }
+    bool ok = run_job(j, st);
+    ok = finish(stg, st, ok);
+    dfree(tmp);  // stream-ordered: the pool hands it out only to later work on this stream
+    if (ok) mark_written(same_view ? (const void *)x->block : (const void *)y->block);
+}
+
+template <typename T, typename VP, typename RMV, typename CMV, typename RB, typename CB>
+static void exec_rc(const VP *vp, const RMV *x, const CMV *z) {
+    Plan *p = plan_of(vp);
+    if (!p || p->type != JV_RCFFTOP) {
+        set_error(E_ARG, "invalid real-to-complex fftm plan");
+        return;
+    }
+    Device *d = device();
+    if (!d) return;
+    std::lock_guard<std::mutex> lk(p->mu);
+    if (!x || !z || !x->block || !z->block) {
+        set_error(E_ARG, "null view");
+        return;
+    }
+    Job j;
+    fill_job(j, p, K_R2C);
+    Geo gx;
+    gx.off = (long)x->offset;
+    gx.es = p->major == 0 ? x->row_stride : x->col_stride;
+    gx.vs = p->major == 0 ? x->col_stride : x->row_stride;
+    gx.len = 2 * p->MN;
+    gx.nvec = p->mN;
+    RRes<T, RB> rx = resolve_r<T, RB>(x->block, gx);
+    CRes<T, CB> rz{z->block, cgeo(z, p->major, p->MN + 1, p->mN), mirror_find(z->block)};
+    Staging stg;
+    cudaStream_t st = d->stream;
+    stage_r(stg, rx, true, false);
+    stage_c(stg, rz, !rz.g.dense(), true);
+    if (!stg.upload(st)) return;
+    j.rin = dev_r(stg, rx);
+    j.cout = dev_c(stg, rz);
+    bool ok = run_job(j, st);
+    ok = finish(stg, st, ok);
+    if (ok) mark_written(z->block);
+}
+
+template <typename T, typename VP, typename CMV, typename RMV, typename CB, typename RB>
+static void exec_cr(const VP *vp, const CMV *z, const RMV *x) {
+    Plan *p = plan_of(vp);
+    if (!p || p->type != JV_CRFFTOP) {
+        set_error(E_ARG, "invalid complex-to-real fftm plan");
+        return;
+    }
+    Device *d = device();
+    if (!d) return;
+    std::lock_guard<std::mutex> lk(p->mu);
+    if (!x || !z || !x->block || !z->block) {
+        set_error(E_ARG, "null view");
+        return;
+    }
+    Job j;
+    fill_job(j, p, K_C2R);
+    Geo gx;
+    gx.off = (long)x->offset;
+    gx.es = p->major == 0 ? x->row_stride : x->col_stride;
+    gx.vs = p->major == 0 ? x->col_stride : x->row_stride;
+    gx.len = 2 * p->MN;
+    gx.nvec = p->mN;
+    RRes<T, RB> rx = resolve_r<T, RB>(x->block, gx);
+    CRes<T, CB> rz{z->block, cgeo(z, p->major, p->MN + 1, p->mN), mirror_find(z->block)};
+    Staging stg;
+    cudaStream_t st = d->stream;
+    stage_c(stg, rz, true, false);
+    stage_r(stg, rx, !rx.g.dense(), true);
+    if (!stg.upload(st)) return;
+    j.cin = dev_c(stg, rz);
+    j.rout = dev_r(stg, rx);
+    bool ok = run_job(j, st);
+    ok = finish(stg, st, ok);
+    if (ok) {
+        if (rx.blk->parent) mark_written(rx.blk->parent);
+        mark_written(rx.blk);
+    }
+}
+
+}  // namespace jv
+
+using namespace jv;
+
+extern "C" {
+
+void vsip_ccfftmop_f(const vsip_fftm_f *p, const vsip_cmview_f *x, const vsip_cmview_f *y) {
+    exec_cc<float, vsip_fftm_f, vsip_cmview_f, vsip_cblock_f>(p, x, y, false);
+}
+void vsip_ccfftmip_f(const vsip_fftm_f *p, const vsip_cmview_f *xy) {
+    exec_cc<float, vsip_fftm_f, vsip_cmview_f, vsip_cblock_f>(p, xy, xy, true);
+}
+void vsip_ccfftmop_d(const vsip_fftm_d *p, const vsip_cmview_d *x, const vsip_cmview_d *y) {
+    exec_cc<double, vsip_fftm_d, vsip_cmview_d, vsip_cblock_d>(p, x, y, false);
+}
+void vsip_ccfftmip_d(const vsip_fftm_d *p, const vsip_cmview_d *xy) {
+    exec_cc<double, vsip_fftm_d, vsip_cmview_d, vsip_cblock_d>(p, xy, xy, true);
+}
+void vsip_rcfftmop_f(const vsip_fftm_f *p, const vsip_mview_f *x, const vsip_cmview_f *z) {
+    exec_rc<float, vsip_fftm_f, vsip_mview_f, vsip_cmview_f, vsip_block_f, vsip_cblock_f>(p, x, z);
+}
+void vsip_rcfftmop_d(const vsip_fftm_d *p, const vsip_mview_d *x, const vsip_cmview_d *z) {
+    exec_rc<double, vsip_fftm_d, vsip_mview_d, vsip_cmview_d, vsip_block_d, vsip_cblock_d>(p, x, z);
+}
+void vsip_crfftmop_f(const vsip_fftm_f *p, const vsip_cmview_f *z, const vsip_mview_f *x) {
+    exec_cr<float, vsip_fftm_f, vsip_cmview_f, vsip_mview_f, vsip_cblock_f, vsip_block_f>(p, z, x);
+}
+void vsip_crfftmop_d(const vsip_fftm_d *p, const vsip_cmview_d *z, const vsip_mview_d *x) {
+    exec_cr<double, vsip_fftm_d, vsip_cmview_d, vsip_mview_d, vsip_cblock_d, vsip_block_d>(p, z, x);
+}
+
+const char *jvsip_gpu_build_info(void) {
+    static char buf[256];
+    Device *d = device();
+    snprintf(buf, sizeof(buf), "jvsip_gb300 fftm: sm_103a kernels; device %d, %d SMs, %zu B smem/block",
+             d ? d->id : -1, d ? d->sms : 0, d ? d->smem_optin : (size_t)0);
+    return buf;
+}
+
+}  // extern "C"

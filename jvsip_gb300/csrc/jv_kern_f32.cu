@@ -1,0 +1,8 @@
+// jv_kern_f32.cu -- single-precision instances of the general kernels.
+#include "jv_launch.cuh"
+
+namespace jv {
+bool launch_smem_f32(const Job &j, cudaStream_t s) { return launch_smem_t<float>(j, s); }
+bool launch_global_f32(const Job &j, cudaStream_t s) { return launch_global_t<float>(j, s); }
+long smem_max_len_f32(int kind) { return smem_len_limit<float>(kind); }
+}  // namespace jv

@@ -1,0 +1,8 @@
+// jv_kern_f64.cu -- double-precision instances of the general kernels.
+#include "jv_launch.cuh"
+
+namespace jv {
+bool launch_smem_f64(const Job &j, cudaStream_t s) { return launch_smem_t<double>(j, s); }
+bool launch_global_f64(const Job &j, cudaStream_t s) { return launch_global_t<double>(j, s); }
+long smem_max_len_f64(int kind) { return smem_len_limit<double>(kind); }
+}  // namespace jv

@@ -1,0 +1,611 @@
+// jv_kernels.cuh -- device code shared by the fftm kernels: complex helpers,
+// the small-DFT codelets, view addressing, and the two general kernels
+//
+//   k_smem : a whole transform (or several) per CTA, resident in shared
+//            memory; self-sorting (Stockham) radix passes 2,3,4,5,7,8,16,
+//            each thread holding its butterflies in registers across the
+//            pass; R2C packing/Hermitian split and C2R un-split are fused into
+//            the load and store phases.
+//   k_gpass: one radix pass over every transform, global memory to global
+//            memory (lengths that do not fit shared memory, or that have a
+//            prime factor above 7).
+//
+// Both compute forward transforms; the inverse runs as conj(F(conj(x))) with
+// the conjugations folded into the load and store of each element.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "jv_core.h"
+
+namespace jv {
+
+template <typename T> struct cplx_t;
+template <> struct cplx_t<float> { typedef float2 t; };
+template <> struct cplx_t<double> { typedef double2 t; };
+
+template <typename C> __device__ __forceinline__ C mk(decltype(C::x) a, decltype(C::x) b) {
+    C r;
+    r.x = a;
+    r.y = b;
+    return r;
+}
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return mk<C>(a.x + b.x, a.y + b.y); }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { return mk<C>(a.x - b.x, a.y - b.y); }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+    return mk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename C> __device__ __forceinline__ C cscale(C a, decltype(C::x) s) { return mk<C>(a.x * s, a.y * s); }
+// multiply by -i
+template <typename C> __device__ __forceinline__ C mul_mi(C a) { return mk<C>(a.y, -a.x); }
+template <typename C> __device__ __forceinline__ C cconj(C a) { return mk<C>(a.x, -a.y); }
+
+// ---------------------------------------------------------------- codelets (forward DFTs)
+// In place on v[0..R-1]: v_k <- sum_n v_n exp(-2 pi i nk/R).
+template <typename C, int R> struct Dft;
+
+template <typename C> struct Dft<C, 2> {
+    static __device__ __forceinline__ void run(C *v) {
+        C a = v[0], b = v[1];
+        v[0] = cadd(a, b);
+        v[1] = csub(a, b);
+    }
+};
+
+template <typename C> struct Dft<C, 4> {
+    static __device__ __forceinline__ void run(C *v) {
+        C s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+        C s13 = cadd(v[1], v[3]), d13 = mul_mi(csub(v[1], v[3]));
+        v[0] = cadd(s02, s13);
+        v[2] = csub(s02, s13);
+        v[1] = cadd(d02, d13);
+        v[3] = csub(d02, d13);
+    }
+};
+
+template <typename C> struct Dft<C, 8> {
+    static __device__ __forceinline__ void run(C *v) {
+        typedef decltype(C::x) T;
+        const T h = (T)0.707106781186547524400844362104849039;
+        C e[4] = {v[0], v[2], v[4], v[6]};
+        C o[4] = {v[1], v[3], v[5], v[7]};
+        Dft<C, 4>::run(e);
+        Dft<C, 4>::run(o);
+        // twiddles exp(-2 pi i k/8), k = 1,2,3
+        C o1 = mk<C>(h * (o[1].x + o[1].y), h * (o[1].y - o[1].x));
+        C o2 = mul_mi(o[2]);
+        C o3 = mk<C>(h * (o[3].y - o[3].x), -h * (o[3].x + o[3].y));
+        v[0] = cadd(e[0], o[0]);
+        v[4] = csub(e[0], o[0]);
+        v[1] = cadd(e[1], o1);
+        v[5] = csub(e[1], o1);
+        v[2] = cadd(e[2], o2);
+        v[6] = csub(e[2], o2);
+        v[3] = cadd(e[3], o3);
+        v[7] = csub(e[3], o3);
+    }
+};
+
+template <typename C> struct Dft<C, 16> {
+    static __device__ __forceinline__ void run(C *v) {
+        typedef decltype(C::x) T;
+        // 4 x 4: columns n1 (stride 4), then twiddle exp(-2 pi i n1 k2/16), then rows
+        const T c1 = (T)0.923879532511286756128183189396788933;  // cos(pi/8)
+        const T s1 = (T)0.382683432365089771728459984030398866;  // sin(pi/8)
+        const T h = (T)0.707106781186547524400844362104849039;
+        C a[4][4];
+#pragma unroll
+        for (int n1 = 0; n1 < 4; n1++) {
+            C t[4] = {v[n1], v[n1 + 4], v[n1 + 8], v[n1 + 12]};
+            Dft<C, 4>::run(t);
+#pragma unroll
+            for (int k2 = 0; k2 < 4; k2++) a[n1][k2] = t[k2];
+        }
+        // twiddles w16^(n1*k2)
+        // n1 = 1: w^0, w^1, w^2, w^3 ; n1 = 2: w^0, w^2, w^4, w^6 ; n1 = 3: w^0, w^3, w^6, w^9
+        a[1][1] = cmul(a[1][1], mk<C>(c1, -s1));
+        a[1][2] = mk<C>(h * (a[1][2].x + a[1][2].y), h * (a[1][2].y - a[1][2].x));
+        a[1][3] = cmul(a[1][3], mk<C>(s1, -c1));
+        a[2][1] = mk<C>(h * (a[2][1].x + a[2][1].y), h * (a[2][1].y - a[2][1].x));
+        a[2][2] = mul_mi(a[2][2]);
+        a[2][3] = mk<C>(h * (a[2][3].y - a[2][3].x), -h * (a[2][3].x + a[2][3].y));
+        a[3][1] = cmul(a[3][1], mk<C>(s1, -c1));
+        a[3][2] = mk<C>(h * (a[3][2].y - a[3][2].x), -h * (a[3][2].x + a[3][2].y));
+        a[3][3] = cmul(a[3][3], mk<C>(-c1, s1));
+#pragma unroll
+        for (int k2 = 0; k2 < 4; k2++) {
+            C t[4] = {a[0][k2], a[1][k2], a[2][k2], a[3][k2]};
+            Dft<C, 4>::run(t);
+#pragma unroll
+            for (int k1 = 0; k1 < 4; k1++) v[k2 + 4 * k1] = t[k1];
+        }
+    }
+};
+
+template <typename C> struct Dft<C, 3> {
+    static __device__ __forceinline__ void run(C *v) {
+        typedef decltype(C::x) T;
+        const T s3 = (T)0.866025403784438646763723170752936183;  // sin(2 pi/3)
+        C s = cadd(v[1], v[2]);
+        C d = csub(v[1], v[2]);
+        C t = mk<C>(v[0].x - (T)0.5 * s.x, v[0].y - (T)0.5 * s.y);
+        C m = mk<C>(s3 * d.y, -s3 * d.x);  // -i sin(2pi/3) d
+        v[0] = cadd(v[0], s);
+        v[1] = cadd(t, m);
+        v[2] = csub(t, m);
+    }
+};
+
+template <typename C> struct Dft<C, 5> {
+    static __device__ __forceinline__ void run(C *v) {
+        typedef decltype(C::x) T;
+        const T c1 = (T)0.309016994374947424102293417182819059;   // cos(2pi/5)
+        const T c2 = (T)-0.809016994374947424102293417182819059;  // cos(4pi/5)
+        const T s1 = (T)0.951056516295153572116439333379382143;   // sin(2pi/5)
+        const T s2 = (T)0.587785252292473129168705954639072769;   // sin(4pi/5)
+        C t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
+        C t3 = csub(v[1], v[4]), t4 = csub(v[2], v[3]);
+        C a0 = v[0];
+        C b1 = mk<C>(a0.x + c1 * t1.x + c2 * t2.x, a0.y + c1 * t1.y + c2 * t2.y);
+        C b2 = mk<C>(a0.x + c2 * t1.x + c1 * t2.x, a0.y + c2 * t1.y + c1 * t2.y);
+        C d1 = mk<C>(s1 * t3.x + s2 * t4.x, s1 * t3.y + s2 * t4.y);
+        C d2 = mk<C>(s2 * t3.x - s1 * t4.x, s2 * t3.y - s1 * t4.y);
+        v[0] = cadd(a0, cadd(t1, t2));
+        // y = b -+ i d
+        v[1] = mk<C>(b1.x + d1.y, b1.y - d1.x);
+        v[4] = mk<C>(b1.x - d1.y, b1.y + d1.x);
+        v[2] = mk<C>(b2.x + d2.y, b2.y - d2.x);
+        v[3] = mk<C>(b2.x - d2.y, b2.y + d2.x);
+    }
+};
+
+template <typename C> struct Dft<C, 7> {
+    static __device__ __forceinline__ void run(C *v) {
+        typedef decltype(C::x) T;
+        const T c1 = (T)0.623489801858733530525004884004239811;   // cos(2pi/7)
+        const T c2 = (T)-0.222520933956314404288902564496794759;  // cos(4pi/7)
+        const T c3 = (T)-0.900968867902419126236102319507445051;  // cos(6pi/7)
+        const T s1 = (T)0.781831482468029808708444526674057751;   // sin(2pi/7)
+        const T s2 = (T)0.974927912181823607018131682993931217;   // sin(4pi/7)
+        const T s3 = (T)0.433883739117558120475768332848358755;   // sin(6pi/7)
+        C a0 = v[0];
+        C p1 = cadd(v[1], v[6]), m1 = csub(v[1], v[6]);
+        C p2 = cadd(v[2], v[5]), m2 = csub(v[2], v[5]);
+        C p3 = cadd(v[3], v[4]), m3 = csub(v[3], v[4]);
+        C b1 = mk<C>(a0.x + c1 * p1.x + c2 * p2.x + c3 * p3.x, a0.y + c1 * p1.y + c2 * p2.y + c3 * p3.y);
+        C b2 = mk<C>(a0.x + c2 * p1.x + c3 * p2.x + c1 * p3.x, a0.y + c2 * p1.y + c3 * p2.y + c1 * p3.y);
+        C b3 = mk<C>(a0.x + c3 * p1.x + c1 * p2.x + c2 * p3.x, a0.y + c3 * p1.y + c1 * p2.y + c2 * p3.y);
+        C d1 = mk<C>(s1 * m1.x + s2 * m2.x + s3 * m3.x, s1 * m1.y + s2 * m2.y + s3 * m3.y);
+        C d2 = mk<C>(s2 * m1.x - s3 * m2.x - s1 * m3.x, s2 * m1.y - s3 * m2.y - s1 * m3.y);
+        C d3 = mk<C>(s3 * m1.x - s1 * m2.x + s2 * m3.x, s3 * m1.y - s1 * m2.y + s2 * m3.y);
+        v[0] = cadd(a0, cadd(p1, cadd(p2, p3)));
+        v[1] = mk<C>(b1.x + d1.y, b1.y - d1.x);
+        v[6] = mk<C>(b1.x - d1.y, b1.y + d1.x);
+        v[2] = mk<C>(b2.x + d2.y, b2.y - d2.x);
+        v[5] = mk<C>(b2.x - d2.y, b2.y + d2.x);
+        v[3] = mk<C>(b3.x + d3.y, b3.y - d3.x);
+        v[4] = mk<C>(b3.x - d3.y, b3.y + d3.x);
+    }
+};
+
+// ---------------------------------------------------------------- view access
+// Complex element (v, n) of a CView; `conj` negates the imaginary part.
+template <typename T> struct CAcc {
+    typedef typename cplx_t<T>::t C;
+    const T *re, *im;
+    long cst, off, es, vs;
+    bool vec;  // interleaved and aligned: one vector load per element
+    __device__ __forceinline__ long idx(long v, long n) const { return cst * (off + v * vs + n * es); }
+    __device__ __forceinline__ C load(long v, long n) const {
+        long i = idx(v, n);
+        if (vec) return *reinterpret_cast<const C *>(re + i);
+        return mk<C>(re[i], im[i]);
+    }
+};
+template <typename T> struct CSto {
+    typedef typename cplx_t<T>::t C;
+    T *re, *im;
+    long cst, off, es, vs;
+    bool vec;
+    __device__ __forceinline__ long idx(long v, long n) const { return cst * (off + v * vs + n * es); }
+    __device__ __forceinline__ void store(long v, long n, C c) const {
+        long i = idx(v, n);
+        if (vec) {
+            *reinterpret_cast<C *>(re + i) = c;
+        } else {
+            re[i] = c.x;
+            im[i] = c.y;
+        }
+    }
+};
+template <typename T> struct RAcc {
+    const T *a;
+    long rst, off, es, vs;
+    __device__ __forceinline__ T load(long v, long n) const { return a[rst * (off + v * vs + n * es)]; }
+};
+template <typename T> struct RSto {
+    T *a;
+    long rst, off, es, vs;
+    __device__ __forceinline__ void store(long v, long n, T x) const { a[rst * (off + v * vs + n * es)] = x; }
+};
+
+// ---------------------------------------------------------------- shared-memory kernel
+template <typename T> struct SmemArgs {
+    typedef typename cplx_t<T>::t C;
+    int kind;         // K_C2C / K_R2C / K_C2R
+    int N;            // complex FFT length
+    int ld;           // shared-memory row pitch (complex elements) >= N (+1 for C2R)
+    int vpb;          // transforms per CTA
+    long nvec;
+    int inv;
+    int has_scale;
+    T scale;
+    int vec_fast;     // global load/store mapping: consecutive threads -> consecutive transforms
+    // pass schedule: n8 radix-8 passes, then n4 radix-4, n2 radix-2, n3 radix-3,
+    // n5 radix-5 and n7 radix-7 passes (a loop per radix keeps register
+    // lifetimes of different codelets apart)
+    int n8, n4, n2, n3, n5, n7;
+    CAcc<T> cin;
+    CSto<T> cout;
+    RAcc<T> rin;
+    RSto<T> rout;
+    const C *tw;      // exp(-2 pi i m/N)
+    const C *thalf;   // exp(-+ i pi k/N), k <= N
+};
+
+// One in-place radix-R pass over the CTA's transforms in shared memory.
+// Butterfly b of transform t reads elements j + r*N/R and writes
+// (j - m)*R + m + r*Ns, m = j mod Ns, after the twiddle exp(-2 pi i r m/(Ns R)).
+// A thread keeps all its butterflies in registers across the barrier, so the
+// pass needs ceil(EMAX/R) * blockDim >= transforms * N/R.
+template <typename T, int R, int EMAX>
+__device__ __forceinline__ void smem_pass(typename cplx_t<T>::t *s, int ld, int N, int nt, int Ns,
+                                          const typename cplx_t<T>::t *__restrict__ tw) {
+    typedef typename cplx_t<T>::t C;
+    constexpr int K = (EMAX + R - 1) / R;
+    const int NR = N / R;
+    const int nb = nt * NR;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    C v[K][R];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        int b = tid + k * nthr;
+        if (b < nb) {
+            int t = b / NR, j = b - t * NR;
+            const C *src = s + t * ld + j;
+#pragma unroll
+            for (int r = 0; r < R; r++) v[k][r] = src[r * NR];
+        }
+    }
+    __syncthreads();
+    const int tstep = N / (Ns * R);
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        int b = tid + k * nthr;
+        if (b < nb) {
+            int t = b / NR, j = b - t * NR;
+            int m = j % Ns;
+            if (m) {
+                int st = m * tstep;
+#pragma unroll
+                for (int r = 1; r < R; r++) v[k][r] = cmul(v[k][r], __ldg(&tw[r * st]));
+            }
+            Dft<C, R>::run(v[k]);
+            C *dst = s + t * ld + (j - m) * R + m;
+#pragma unroll
+            for (int r = 0; r < R; r++) dst[r * Ns] = v[k][r];
+        }
+    }
+    __syncthreads();
+}
+
+template <typename T, int EMAX>
+__device__ __forceinline__ void smem_passes(typename cplx_t<T>::t *s, int ld, int N, int nt, int n8, int n4,
+                                            int n2, int n3, int n5, int n7,
+                                            const typename cplx_t<T>::t *__restrict__ tw) {
+    int Ns = 1;
+    for (int p = 0; p < n8; p++) { smem_pass<T, 8, EMAX>(s, ld, N, nt, Ns, tw); Ns *= 8; }
+    for (int p = 0; p < n4; p++) { smem_pass<T, 4, EMAX>(s, ld, N, nt, Ns, tw); Ns *= 4; }
+    for (int p = 0; p < n2; p++) { smem_pass<T, 2, EMAX>(s, ld, N, nt, Ns, tw); Ns *= 2; }
+    for (int p = 0; p < n3; p++) { smem_pass<T, 3, EMAX>(s, ld, N, nt, Ns, tw); Ns *= 3; }
+    for (int p = 0; p < n5; p++) { smem_pass<T, 5, EMAX>(s, ld, N, nt, Ns, tw); Ns *= 5; }
+    for (int p = 0; p < n7; p++) { smem_pass<T, 7, EMAX>(s, ld, N, nt, Ns, tw); Ns *= 7; }
+}
+
+template <typename T, int EMAX, int MAXT>
+__global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
+    typedef typename cplx_t<T>::t C;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *s = reinterpret_cast<C *>(smem_raw);
+    const int N = a.N, ld = a.ld;
+    // register copies: member calls on kernel-parameter structs would force local copies
+    const CAcc<T> cin = a.cin;
+    const CSto<T> cout = a.cout;
+    const RAcc<T> rin = a.rin;
+    const RSto<T> rout = a.rout;
+    const C *__restrict__ thalf = a.thalf;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const long ngroups = (a.nvec + a.vpb - 1) / a.vpb;
+    {
+        // one CTA per group of transforms (a grid-stride loop around the
+        // barrier-separated passes makes ptxas spill the codelet registers)
+        const long g = blockIdx.x;
+        if (g >= ngroups) return;
+        const long v0 = g * a.vpb;
+        const int nt = (int)min((long)a.vpb, a.nvec - v0);
+        // ---------------- load phase
+        if (a.kind == K_C2C) {
+            const int tot = nt * N;
+            for (int i = tid; i < tot; i += nthr) {
+                int t, n;
+                if (a.vec_fast) { t = i % nt; n = i / nt; } else { t = i / N; n = i - t * N; }
+                C c = cin.load(v0 + t, n);
+                if (a.inv) c.y = -c.y;
+                s[t * ld + n] = c;
+            }
+        } else if (a.kind == K_R2C) {
+            // z_n = x_{2n} + i x_{2n+1}  (c_VSIP_src/VI_rcfftmop_f_def.h:53-75)
+            const int tot = nt * N;
+            for (int i = tid; i < tot; i += nthr) {
+                int t, n;
+                if (a.vec_fast) { t = i % nt; n = i / nt; } else { t = i / N; n = i - t * N; }
+                s[t * ld + n] = mk<C>(rin.load(v0 + t, 2 * n), rin.load(v0 + t, 2 * n + 1));
+            }
+        } else {
+            // C2R: raw Z_k, k <= N, then the inverse split (VI_crfftmop_f_def.h:58-110)
+            const int tot = nt * (N + 1);
+            for (int i = tid; i < tot; i += nthr) {
+                int t, k;
+                if (a.vec_fast) { t = i % nt; k = i / nt; } else { t = i / (N + 1); k = i - t * (N + 1); }
+                s[t * ld + k] = cin.load(v0 + t, k);
+            }
+            __syncthreads();
+            const int half = N / 2 + 1;   // pairs (k, N-k), k = 0..N/2
+            const int totp = nt * half;
+            for (int i = tid; i < totp; i += nthr) {
+                int t = i / half, k = i - t * half;
+                C *row = s + t * ld;
+                C f = row[k], b = row[N - k];
+                C w = thalf[k];
+                // Y_k = f + b + w.i (b - f) ... with f = Z_k, b = Z_{N-k}, w = exp(+i pi k/N)
+                C yk = mk<C>(f.x + b.x + w.y * (b.x - f.x) - w.x * (f.y + b.y),
+                             f.y - b.y - w.y * (f.y + b.y) + w.x * (f.x - b.x));
+                C yn;
+                bool pair = (k != 0) && (N - k != k);
+                if (pair) {
+                    C w2 = thalf[N - k];
+                    yn = mk<C>(b.x + f.x + w2.y * (f.x - b.x) - w2.x * (b.y + f.y),
+                               b.y - f.y - w2.y * (b.y + f.y) + w2.x * (b.x - f.x));
+                }
+                // the inverse transform runs as a forward one on conjugated data
+                row[k] = mk<C>(yk.x, -yk.y);
+                if (pair) row[N - k] = mk<C>(yn.x, -yn.y);
+            }
+        }
+        __syncthreads();
+        // ---------------- radix passes
+        smem_passes<T, EMAX>(s, ld, N, nt, a.n8, a.n4, a.n2, a.n3, a.n5, a.n7, a.tw);
+        // ---------------- store phase
+        if (a.kind == K_C2C) {
+            const int tot = nt * N;
+            for (int i = tid; i < tot; i += nthr) {
+                int t, n;
+                if (a.vec_fast) { t = i % nt; n = i / nt; } else { t = i / N; n = i - t * N; }
+                C c = s[t * ld + n];
+                if (a.inv) c.y = -c.y;
+                if (a.has_scale) c = cscale(c, a.scale);
+                cout.store(v0 + t, n, c);
+            }
+        } else if (a.kind == K_R2C) {
+            // Hermitian split (VI_rcfftmop_f_def.h:79-118): X_k from Z_k and Z_{N-k} (Z_N = Z_0)
+            const int tot = nt * (N + 1);
+            for (int i = tid; i < tot; i += nthr) {
+                int t, k;
+                if (a.vec_fast) { t = i % nt; k = i / nt; } else { t = i / (N + 1); k = i - t * (N + 1); }
+                const C *row = s + t * ld;
+                C f = row[k == N ? 0 : k];
+                C b = row[k == 0 ? 0 : N - k];
+                if (a.has_scale) {
+                    f = cscale(f, a.scale);
+                    b = cscale(b, a.scale);
+                }
+                C w = thalf[k];
+                C x = mk<C>((T)0.5 * (b.x + f.x + w.x * (b.y + f.y) + w.y * (f.x - b.x)),
+                            (T)0.5 * (f.y - b.y + w.x * (b.x - f.x) + w.y * (b.y + f.y)));
+                cout.store(v0 + t, k, x);
+            }
+        } else {
+            // x_{2n} = Re y_n, x_{2n+1} = Im y_n (VI_crfftmop_f_def.h:121-124)
+            const int tot = nt * N;
+            for (int i = tid; i < tot; i += nthr) {
+                int t, n;
+                if (a.vec_fast) { t = i % nt; n = i / nt; } else { t = i / N; n = i - t * N; }
+                C c = s[t * ld + n];
+                T re = c.x, im = -c.y;
+                if (a.has_scale) {
+                    re *= a.scale;
+                    im *= a.scale;
+                }
+                rout.store(v0 + t, 2 * n, re);
+                rout.store(v0 + t, 2 * n + 1, im);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- global pass kernel
+// One radix-R pass of every transform: src -> dst, both given as views in
+// transform order.  R is a codelet radix or any odd prime (O(R^2) direct sum).
+template <typename T> struct GPassArgs {
+    typedef typename cplx_t<T>::t C;
+    int N, R, Ns;
+    long nvec;
+    int conj_in, conj_out;  // conjugate on read / write
+    int has_scale;
+    T scale;
+    int src_real;           // src is a real view read as z_n = x_2n + i x_2n+1
+    CAcc<T> src;
+    RAcc<T> rsrc;
+    CSto<T> dst;
+    const C *tw;
+};
+
+template <typename T, int R>
+__device__ __forceinline__ void gpass_body(const GPassArgs<T> &a, long v, int j) {
+    typedef typename cplx_t<T>::t C;
+    const int NR = a.N / R;
+    C x[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        C c;
+        if (a.src_real) c = mk<C>(a.rsrc.load(v, 2 * (j + r * NR)), a.rsrc.load(v, 2 * (j + r * NR) + 1));
+        else c = a.src.load(v, j + r * NR);
+        if (a.conj_in) c.y = -c.y;
+        x[r] = c;
+    }
+    int m = j % a.Ns;
+    if (m) {
+        long st = (long)m * (a.N / (a.Ns * R));
+#pragma unroll
+        for (int r = 1; r < R; r++) x[r] = cmul(x[r], __ldg(&a.tw[r * st]));
+    }
+    Dft<C, R>::run(x);
+    long base = (long)(j - m) * R + m;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        C c = x[r];
+        if (a.conj_out) c.y = -c.y;
+        if (a.has_scale) c = cscale(c, a.scale);
+        a.dst.store(v, base + (long)r * a.Ns, c);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void gpass_generic(const GPassArgs<T> &a, long v, int j) {
+    typedef typename cplx_t<T>::t C;
+    const int R = a.R, NR = a.N / R;
+    int m = j % a.Ns;
+    long st = (long)m * (a.N / (a.Ns * R));
+    long base = (long)(j - m) * R + m;
+    const long rstep = a.N / R;  // table index step of exp(-2 pi i/R)
+    for (int k = 0; k < R; k++) {
+        C acc = mk<C>((T)0, (T)0);
+        for (int n = 0; n < R; n++) {
+            C c;
+            if (a.src_real) c = mk<C>(a.rsrc.load(v, 2 * (j + n * NR)), a.rsrc.load(v, 2 * (j + n * NR) + 1));
+            else c = a.src.load(v, j + n * NR);
+            if (a.conj_in) c.y = -c.y;
+            if (m && n) c = cmul(c, __ldg(&a.tw[n * st]));
+            long e = ((long)n * k) % R;
+            C w = __ldg(&a.tw[e * rstep]);
+            acc = cadd(acc, cmul(c, w));
+        }
+        if (a.conj_out) acc.y = -acc.y;
+        if (a.has_scale) acc = cscale(acc, a.scale);
+        a.dst.store(v, base + (long)k * a.Ns, acc);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_gpass(const GPassArgs<T> pa) {
+    const GPassArgs<T> a = pa;
+    const long NR = a.N / a.R;
+    const long total = a.nvec * NR;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        long v = i / NR;
+        int j = (int)(i - v * NR);
+        switch (a.R) {
+            case 2: gpass_body<T, 2>(a, v, j); break;
+            case 3: gpass_body<T, 3>(a, v, j); break;
+            case 4: gpass_body<T, 4>(a, v, j); break;
+            case 5: gpass_body<T, 5>(a, v, j); break;
+            case 7: gpass_body<T, 7>(a, v, j); break;
+            case 8: gpass_body<T, 8>(a, v, j); break;
+            case 16: gpass_body<T, 16>(a, v, j); break;
+            default: gpass_generic<T>(a, v, j); break;
+        }
+    }
+}
+
+// R2C Hermitian split / C2R un-split on dense scratch for the global path.
+template <typename T> struct SplitArgs {
+    typedef typename cplx_t<T>::t C;
+    int N;          // half length MN
+    long nvec;
+    int has_scale;
+    T scale;
+    const C *zsrc;  // R2C: transformed Z (dense [nvec][N]); C2R: unused
+    CAcc<T> zin;    // C2R: input spectrum view (N+1 per transform)
+    CSto<T> xout;   // R2C: output spectrum view (N+1 per transform)
+    C *ydst;        // C2R: dense [nvec][N] conjugated Y for the forward passes
+    const C *thalf;
+};
+
+template <typename T>
+__global__ void k_r2c_split(const SplitArgs<T> a) {
+    typedef typename cplx_t<T>::t C;
+    const long tot = a.nvec * (a.N + 1);
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < tot; i += (long)gridDim.x * blockDim.x) {
+        long v = i / (a.N + 1);
+        int k = (int)(i - v * (a.N + 1));
+        const C *row = a.zsrc + v * a.N;
+        C f = row[k == a.N ? 0 : k];
+        C b = row[k == 0 ? 0 : a.N - k];
+        if (a.has_scale) {
+            f = cscale(f, a.scale);
+            b = cscale(b, a.scale);
+        }
+        C w = a.thalf[k];
+        C x = mk<C>((T)0.5 * (b.x + f.x + w.x * (b.y + f.y) + w.y * (f.x - b.x)),
+                    (T)0.5 * (f.y - b.y + w.x * (b.x - f.x) + w.y * (b.y + f.y)));
+        a.xout.store(v, k, x);
+    }
+}
+
+template <typename T>
+__global__ void k_c2r_unsplit(const SplitArgs<T> a) {
+    typedef typename cplx_t<T>::t C;
+    const long tot = a.nvec * a.N;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < tot; i += (long)gridDim.x * blockDim.x) {
+        long v = i / a.N;
+        int k = (int)(i - v * a.N);
+        C f = a.zin.load(v, k), b = a.zin.load(v, a.N - k);
+        C w = a.thalf[k];
+        C y = mk<C>(f.x + b.x + w.y * (b.x - f.x) - w.x * (f.y + b.y),
+                    f.y - b.y - w.y * (f.y + b.y) + w.x * (f.x - b.x));
+        a.ydst[v * a.N + k] = mk<C>(y.x, -y.y);
+    }
+}
+
+// C2R final store from dense conjugated y: x_2n = Re, x_2n+1 = -Im (conj back), scaled.
+template <typename T> struct UnpackArgs {
+    typedef typename cplx_t<T>::t C;
+    int N;
+    long nvec;
+    int has_scale;
+    T scale;
+    const C *y;
+    RSto<T> xout;
+};
+
+template <typename T>
+__global__ void k_c2r_unpack(const UnpackArgs<T> a) {
+    typedef typename cplx_t<T>::t C;
+    const long tot = a.nvec * a.N;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < tot; i += (long)gridDim.x * blockDim.x) {
+        long v = i / a.N;
+        int n = (int)(i - v * a.N);
+        C c = a.y[i];
+        T re = c.x, im = -c.y;
+        if (a.has_scale) {
+            re *= a.scale;
+            im *= a.scale;
+        }
+        a.xout.store(v, 2 * n, re);
+        a.xout.store(v, 2 * n + 1, im);
+    }
+}
+
+}  // namespace jv

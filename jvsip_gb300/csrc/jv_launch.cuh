@@ -1,0 +1,381 @@
+// jv_launch.cuh -- host-side launchers of the general kernels, written once
+// for both precisions and instantiated in jv_kern_f32.cu / jv_kern_f64.cu.
+#pragma once
+
+#include <stdio.h>
+
+#include "jv_kernels.cuh"
+
+namespace jv {
+
+// Two register budgets of the shared-memory kernel per precision: EMAX complex
+// values a thread keeps per radix pass and the block size bound MAXT.  The
+// small variant serves transforms of up to EMAX*MAXT/2 elements per CTA
+// without spilling; the large one reaches EMAX*MAXT elements.
+template <typename T> struct KCfg;
+template <> struct KCfg<float> {
+    static constexpr int EMAX_S = 8, MAXT_S = 1024, EMAX_L = 16, MAXT_L = 1024;
+};
+template <> struct KCfg<double> {
+    static constexpr int EMAX_S = 8, MAXT_S = 512, EMAX_L = 16, MAXT_L = 512;
+};
+
+template <typename T>
+static CAcc<T> cacc(const CView &v) {
+    CAcc<T> a;
+    a.re = (const T *)v.re;
+    a.im = (const T *)v.im;
+    a.cst = v.cst;
+    a.off = v.off;
+    a.es = v.es;
+    a.vs = v.vs;
+    a.vec = (v.cst == 2) && ((const T *)v.im == (const T *)v.re + 1) &&
+            (((uintptr_t)v.re % (2 * sizeof(T))) == 0);
+    return a;
+}
+template <typename T>
+static CSto<T> csto(const CView &v) {
+    CSto<T> a;
+    a.re = (T *)v.re;
+    a.im = (T *)v.im;
+    a.cst = v.cst;
+    a.off = v.off;
+    a.es = v.es;
+    a.vs = v.vs;
+    a.vec = (v.cst == 2) && ((T *)v.im == (T *)v.re + 1) && (((uintptr_t)v.re % (2 * sizeof(T))) == 0);
+    return a;
+}
+template <typename T>
+static RAcc<T> racc(const RView &v) {
+    RAcc<T> a;
+    a.a = (const T *)v.a;
+    a.rst = v.rst;
+    a.off = v.off;
+    a.es = v.es;
+    a.vs = v.vs;
+    return a;
+}
+template <typename T>
+static RSto<T> rsto(const RView &v) {
+    RSto<T> a;
+    a.a = (T *)v.a;
+    a.rst = v.rst;
+    a.off = v.off;
+    a.es = v.es;
+    a.vs = v.vs;
+    return a;
+}
+
+static inline long labs_(long x) { return x < 0 ? -x : x; }
+
+template <typename T>
+long smem_len_limit(int kind) {
+    Device *d = device();
+    size_t cap = d ? d->smem_optin : 48 * 1024;
+    long byfit = (long)(cap / (2 * sizeof(T))) - 2;
+    long bythreads = (long)KCfg<T>::EMAX_L * KCfg<T>::MAXT_L;
+    long lim = byfit < bythreads ? byfit : bythreads;
+    (void)kind;
+    return lim;
+}
+
+// Threads needed so that every pass fits: a thread holds ceil(EMAX/R)
+// butterflies of radix R.
+template <int EMAX>
+static long threads_needed(const Job &j, long elems) {
+    long need = 32;
+    for (int i = 0; i < j.npass; i++) {
+        long R = j.radix[i];
+        long K = (EMAX + R - 1) / R;
+        long t = (elems / R + K - 1) / K;
+        if (t > need) need = t;
+    }
+    return ((need + 31) / 32) * 32;
+}
+
+template <typename T, int EMAX, int MAXT>
+static bool launch_smem_v(SmemArgs<T> &a, const Job &j, long vpb, long ld, cudaStream_t st) {
+    typedef typename cplx_t<T>::t C;
+    Device *d = device();
+    long nthr = threads_needed<EMAX>(j, vpb * j.N);
+    if (nthr < 64) nthr = 64;
+    if (nthr > MAXT) {
+        set_error(E_UNSUPPORTED, "transform too large for the shared-memory kernel");
+        return false;
+    }
+    a.vpb = (int)vpb;
+    a.ld = (int)ld;
+    size_t smem = (size_t)vpb * ld * sizeof(C);
+    static bool attr_set = false;
+    if (!attr_set) {
+        if (!cuda_ok(cudaFuncSetAttribute(k_smem<T, EMAX, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)d->smem_optin),
+                     "cudaFuncSetAttribute"))
+            return false;
+        attr_set = true;
+    }
+    long grid = (j.nvec + vpb - 1) / vpb;
+    if (grid > 0x7fffffffL) {
+        set_error(E_UNSUPPORTED, "too many transforms for one launch");
+        return false;
+    }
+    k_smem<T, EMAX, MAXT><<<(unsigned)grid, (unsigned)nthr, smem, st>>>(a);
+    return cuda_ok(cudaGetLastError(), "k_smem launch");
+}
+
+template <typename T>
+bool launch_smem_t(const Job &j, cudaStream_t st) {
+    typedef typename cplx_t<T>::t C;
+    typedef KCfg<T> K;
+    Device *d = device();
+    if (!d) return false;
+    if (j.nvec <= 0 || j.N <= 0) return true;
+    SmemArgs<T> a;
+    memset(&a, 0, sizeof(a));
+    a.kind = j.kind;
+    a.N = (int)j.N;
+    a.nvec = j.nvec;
+    a.inv = j.inv;
+    a.has_scale = j.has_scale;
+    a.scale = (T)j.scale;
+    // the plan lists its radices in the kernel's order: 8s, 4, 2, 3s, 5s, 7s
+    for (int i = 0; i < j.npass; i++) {
+        switch (j.radix[i]) {
+            case 8: a.n8++; break;
+            case 4: a.n4++; break;
+            case 2: a.n2++; break;
+            case 3: a.n3++; break;
+            case 5: a.n5++; break;
+            case 7: a.n7++; break;
+            default: set_error(E_UNSUPPORTED, "radix not handled by the shared-memory kernel"); return false;
+        }
+    }
+    a.cin = cacc<T>(j.cin);
+    a.cout = csto<T>(j.cout);
+    a.rin = racc<T>(j.rin);
+    a.rout = rsto<T>(j.rout);
+    a.tw = (const C *)j.tw;
+    a.thalf = (const C *)j.thalf;
+    // global access mapping: when consecutive transforms are adjacent in memory
+    // (column transforms of a row-major matrix) consecutive threads take
+    // consecutive transforms, otherwise consecutive elements of one transform.
+    long es_in = (j.kind == K_R2C) ? j.rin.es : j.cin.es, vs_in = (j.kind == K_R2C) ? j.rin.vs : j.cin.vs;
+    long es_out = (j.kind == K_C2R) ? j.rout.es : j.cout.es, vs_out = (j.kind == K_C2R) ? j.rout.vs : j.cout.vs;
+    bool vf_in = labs_(vs_in) == 1 && labs_(es_in) != 1;
+    bool vf_out = labs_(vs_out) == 1 && labs_(es_out) != 1;
+    a.vec_fast = (vf_in || vf_out) ? 1 : 0;
+    const long N = j.N;
+    long ld = N + (j.kind == K_C2R ? 1 : 0);
+    const long elem_cap = (long)K::EMAX_L * K::MAXT_L;
+    long vpb;
+    if (a.vec_fast) {
+        vpb = (sizeof(T) == 4) ? 16 : 8;
+        if (ld % 2 == 0) ld += 1;
+    } else {
+        long target = (sizeof(T) == 4) ? 2048 : 1024;
+        vpb = target / N;
+        if (vpb < 1) vpb = 1;
+    }
+    size_t cap = d->smem_optin;
+    while (vpb > 1 && ((size_t)vpb * ld * sizeof(C) > cap || vpb * N > elem_cap)) vpb--;
+    if (vpb > j.nvec) vpb = j.nvec;
+    if ((size_t)vpb * ld * sizeof(C) > cap || vpb * N > elem_cap) {
+        set_error(E_UNSUPPORTED, "length too large for the shared-memory kernel");
+        return false;
+    }
+    if (threads_needed<K::EMAX_S>(j, vpb * N) <= K::MAXT_S)
+        return launch_smem_v<T, K::EMAX_S, K::MAXT_S>(a, j, vpb, ld, st);
+    return launch_smem_v<T, K::EMAX_L, K::MAXT_L>(a, j, vpb, ld, st);
+}
+
+template <typename T>
+static CView dense_view(void *buf, long N) {
+    CView v;
+    v.re = buf;
+    v.im = (T *)buf + 1;
+    v.cst = 2;
+    v.off = 0;
+    v.es = 1;
+    v.vs = N;
+    return v;
+}
+
+template <typename T>
+static bool gpass(const GPassArgs<T> &a, cudaStream_t st) {
+    Device *d = device();
+    long total = a.nvec * (a.N / a.R);
+    long grid = (total + 255) / 256;
+    long gmax = (long)d->sms * 32;
+    if (grid > gmax) grid = gmax;
+    if (grid < 1) grid = 1;
+    k_gpass<T><<<(unsigned)grid, 256, 0, st>>>(a);
+    return cuda_ok(cudaGetLastError(), "k_gpass launch");
+}
+
+template <typename T>
+static unsigned grid_for(long total) {
+    Device *d = device();
+    long g = (total + 255) / 256;
+    long gmax = (long)d->sms * 32;
+    if (g > gmax) g = gmax;
+    if (g < 1) g = 1;
+    return (unsigned)g;
+}
+
+// Global-memory path: one launch per radix pass, dense scratch between passes.
+template <typename T>
+bool launch_global_t(const Job &j, cudaStream_t st) {
+    typedef typename cplx_t<T>::t C;
+    if (j.nvec <= 0 || j.N <= 0) return true;
+    const long N = j.N;
+    const size_t bytes = (size_t)j.nvec * N * sizeof(C);
+    void *A = dmalloc(bytes), *B = dmalloc(bytes);
+    if (!A || !B) {
+        dfree(A);
+        dfree(B);
+        return false;
+    }
+    bool ok = true;
+    GPassArgs<T> g;
+    memset(&g, 0, sizeof(g));
+    g.N = (int)N;
+    g.nvec = j.nvec;
+    g.tw = (const C *)j.tw;
+    void *cur = A, *nxt = B;
+    if (j.kind == K_C2C) {
+        const int np = j.npass;
+        if (np == 0) {
+            // length-1 transform: a radix-1 pass is a copy with scale
+            GPassArgs<T> a = g;
+            a.R = 1;
+            a.Ns = 1;
+            a.src = cacc<T>(j.cin);
+            a.dst = csto<T>(j.cout);
+            a.has_scale = j.has_scale;
+            a.scale = (T)j.scale;
+            ok = gpass<T>(a, st);
+        }
+        int Ns = 1;
+        for (int p = 0; p < np && ok; p++) {
+            GPassArgs<T> a = g;
+            a.R = j.radix[p];
+            a.Ns = Ns;
+            bool first = (p == 0), last = (p == np - 1);
+            a.src = first ? cacc<T>(j.cin) : cacc<T>(dense_view<T>(cur, N));
+            a.conj_in = first && j.inv;
+            bool to_out = last && !(j.inplace && np == 1);
+            if (to_out) {
+                a.dst = csto<T>(j.cout);
+                a.conj_out = j.inv;
+                a.has_scale = j.has_scale;
+                a.scale = (T)j.scale;
+            } else {
+                a.dst = csto<T>(dense_view<T>(first ? cur : nxt, N));
+            }
+            ok = gpass<T>(a, st);
+            if (!first) {
+                void *t = cur;
+                cur = nxt;
+                nxt = t;
+            }
+            Ns *= j.radix[p];
+        }
+        if (ok && j.inplace && np == 1) {
+            // single pass in place: the pass wrote scratch, a radix-1 copy finishes
+            GPassArgs<T> a = g;
+            a.R = 1;
+            a.Ns = 1;
+            a.src = cacc<T>(dense_view<T>(cur, N));
+            a.dst = csto<T>(j.cout);
+            a.conj_out = j.inv;
+            a.has_scale = j.has_scale;
+            a.scale = (T)j.scale;
+            ok = gpass<T>(a, st);
+        }
+    } else if (j.kind == K_R2C) {
+        int Ns = 1;
+        for (int p = 0; p < j.npass && ok; p++) {
+            GPassArgs<T> a = g;
+            a.R = j.radix[p];
+            a.Ns = Ns;
+            if (p == 0) {
+                a.src_real = 1;
+                a.rsrc = racc<T>(j.rin);
+                a.dst = csto<T>(dense_view<T>(cur, N));
+            } else {
+                a.src = cacc<T>(dense_view<T>(cur, N));
+                a.dst = csto<T>(dense_view<T>(nxt, N));
+            }
+            ok = gpass<T>(a, st);
+            if (p > 0) {
+                void *t = cur;
+                cur = nxt;
+                nxt = t;
+            }
+            Ns *= j.radix[p];
+        }
+        if (ok && j.npass == 0) {  // MN = 1: pack only
+            GPassArgs<T> a = g;
+            a.R = 1;
+            a.Ns = 1;
+            a.src_real = 1;
+            a.rsrc = racc<T>(j.rin);
+            a.dst = csto<T>(dense_view<T>(cur, N));
+            ok = gpass<T>(a, st);
+        }
+        if (ok) {
+            SplitArgs<T> s;
+            memset(&s, 0, sizeof(s));
+            s.N = (int)N;
+            s.nvec = j.nvec;
+            s.has_scale = j.has_scale;
+            s.scale = (T)j.scale;
+            s.zsrc = (const C *)cur;
+            s.xout = csto<T>(j.cout);
+            s.thalf = (const C *)j.thalf;
+            k_r2c_split<T><<<grid_for<T>(j.nvec * (N + 1)), 256, 0, st>>>(s);
+            ok = cuda_ok(cudaGetLastError(), "k_r2c_split launch");
+        }
+    } else {
+        SplitArgs<T> s;
+        memset(&s, 0, sizeof(s));
+        s.N = (int)N;
+        s.nvec = j.nvec;
+        s.zin = cacc<T>(j.cin);
+        s.ydst = (C *)cur;
+        s.thalf = (const C *)j.thalf;
+        k_c2r_unsplit<T><<<grid_for<T>(j.nvec * N), 256, 0, st>>>(s);
+        ok = cuda_ok(cudaGetLastError(), "k_c2r_unsplit launch");
+        int Ns = 1;
+        for (int p = 0; p < j.npass && ok; p++) {
+            GPassArgs<T> a = g;
+            a.R = j.radix[p];
+            a.Ns = Ns;
+            a.src = cacc<T>(dense_view<T>(cur, N));
+            a.dst = csto<T>(dense_view<T>(nxt, N));
+            ok = gpass<T>(a, st);
+            void *t = cur;
+            cur = nxt;
+            nxt = t;
+            Ns *= j.radix[p];
+        }
+        if (ok) {
+            UnpackArgs<T> u;
+            memset(&u, 0, sizeof(u));
+            u.N = (int)N;
+            u.nvec = j.nvec;
+            u.has_scale = j.has_scale;
+            u.scale = (T)j.scale;
+            u.y = (const C *)cur;
+            u.xout = rsto<T>(j.rout);
+            k_c2r_unpack<T><<<grid_for<T>(j.nvec * N), 256, 0, st>>>(u);
+            ok = cuda_ok(cudaGetLastError(), "k_c2r_unpack launch");
+        }
+    }
+    // scratch goes back to the pool; reuse is ordered on the library stream
+    dfree(A);
+    dfree(B);
+    return ok;
+}
+
+}  // namespace jv

@@ -1,0 +1,334 @@
+// jv_plan.cu -- multiple-FFT plans: vsip_{cc,rc,cr}fftm{op,ip}_create_{f,d},
+// vsip_fftm_destroy_{f,d}, vsip_fftm_getattr_{f,d}.
+//
+// A plan is the reference's plan object (layout of
+// c_VSIP_src/vsip_fftmattributes_f.h:8-38, attributes filled with the
+// reference's meaning, c_VSIP_src/VI_ccfftmop_create_f_def.h:23-88,
+// VI_rcfftmop_create_f_def.h:26-99, VI_crfftmop_create_f_def.h:24-96) whose
+// ext_fftm_obj points to the device plan: the pass schedule of the kernels,
+// the device twiddle tables (generated in FP64, rounded to the plan's type)
+// and, for real transforms, the half-angle table exp(-+ i pi k/MN).
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <new>
+
+#include "jv_core.h"
+
+namespace jv {
+
+unsigned long ref_factor(unsigned long N, unsigned long *pn, unsigned long *p0, unsigned long *pF) {
+    // c_VSIP_src/VI_nuV.h:22-136: radices in the order 3, 5, 7, 8, 4, 2; the
+    // cofactor left after a radix is that stage's final radix.
+    static const unsigned long order[6] = {3, 5, 7, 8, 4, 2};
+    unsigned long n = N, k = 0;
+    if (N == 0) return 0;
+    for (int r = 0; r < 6; r++) {
+        unsigned long q = order[r], c = 0;
+        while (n % q == 0) {
+            n /= q;
+            c++;
+        }
+        if (c) {
+            p0[k] = q;
+            pF[k] = (n != 1) ? n : q;
+            pn[k] = (n != 1) ? c + 1 : c;
+            k++;
+        }
+    }
+    if (n != 1 && k == 0) {
+        p0[0] = 1;
+        pF[0] = n;
+        pn[0] = 1;
+        k = 1;
+    }
+    return k;
+}
+
+static unsigned long ref_jofk(unsigned long k, const unsigned long *pn, const unsigned long *p0,
+                              unsigned long pF, unsigned long ns) {
+    // c_VSIP_src/VI_jofk.h:21-48
+    unsigned long j = 0, m = k;
+    for (unsigned long q = 0; q < ns; q++)
+        for (unsigned long i = 1; i < pn[q]; i++) {
+            unsigned long s = m / p0[q];
+            j = p0[q] * j + (m - s * p0[q]);
+            m = s;
+        }
+    unsigned long s = m / pF;
+    return pF * j + (m - s * pF);
+}
+
+std::vector<int> pass_radices(long N, bool *smooth) {
+    std::vector<int> r;
+    *smooth = true;
+    if (N <= 1) return r;
+    long n = N;
+    int twos = 0;
+    while (n % 2 == 0) {
+        n /= 2;
+        twos++;
+    }
+    // powers of two: radix-8 passes, the remainder as one radix-4 or radix-2 pass
+    while (twos >= 3) {
+        r.push_back(8);
+        twos -= 3;
+    }
+    if (twos == 2) r.push_back(4);
+    if (twos == 1) r.push_back(2);
+    for (int p : {3, 5, 7}) {
+        while (n % p == 0) {
+            n /= p;
+            r.push_back(p);
+        }
+    }
+    for (long p = 11; n > 1 && p * p <= n; p += 2) {
+        while (n % p == 0) {
+            n /= p;
+            r.push_back((int)p);
+            *smooth = false;
+        }
+    }
+    if (n > 1) {
+        r.push_back((int)n);
+        *smooth = false;
+    }
+    return r;
+}
+
+// exp(-2 pi i m/N) in double with the angle reduced to [0, pi] by symmetry
+static void unit_root(long m, long N, double *c, double *s) {
+    bool flip = false;
+    if (2 * m > N) {
+        m = N - m;
+        flip = true;
+    }
+    double x = (double)m / (double)N;
+    double a = 2.0 * 3.14159265358979323846264338327950288 * x;
+    *c = cos(a);
+    double sn = sin(a);
+    *s = flip ? sn : -sn;
+}
+
+template <typename T>
+static bool make_tables(Plan *p) {
+    long MN = p->MN;
+    size_t n = (size_t)(MN > 0 ? MN : 1);
+    std::vector<T> tw(2 * n, (T)0);
+    for (long m = 0; m < MN; m++) {
+        double c, s;
+        unit_root(m, MN, &c, &s);
+        tw[2 * m] = (T)c;
+        tw[2 * m + 1] = (T)s;
+    }
+    Device *d = device();
+    if (!d) return false;
+    p->d_tw = dmalloc(2 * n * sizeof(T));
+    if (!p->d_tw) return false;
+    if (!cuda_ok(cudaMemcpy(p->d_tw, tw.data(), 2 * n * sizeof(T), cudaMemcpyHostToDevice), "twiddle upload"))
+        return false;
+    if (p->type == JV_RCFFTOP || p->type == JV_CRFFTOP) {
+        // exp(-i pi k/MN) for R2C, exp(+i pi k/MN) for C2R, k = 0..MN
+        // (c_VSIP_src/VI_rcfftmop_create_f_def.h:75-86, VI_crfftmop_create_f_def.h:72-83)
+        std::vector<T> th(2 * (n + 1));
+        for (long k = 0; k <= MN; k++) {
+            double c, s;
+            unit_root(k, 2 * MN, &c, &s);  // exp(-i pi k/MN)
+            th[2 * k] = (T)c;
+            th[2 * k + 1] = (T)((p->type == JV_RCFFTOP) ? s : -s);
+        }
+        p->d_thalf = dmalloc(2 * (n + 1) * sizeof(T));
+        if (!p->d_thalf) return false;
+        if (!cuda_ok(cudaMemcpy(p->d_thalf, th.data(), 2 * (n + 1) * sizeof(T), cudaMemcpyHostToDevice),
+                     "half-angle table upload"))
+            return false;
+    }
+    return true;
+}
+
+static void plan_free(Plan *p) {
+    if (!p) return;
+    Device *d = device();
+    if (d) cudaStreamSynchronize(d->stream);
+    dfree(p->d_tw);
+    dfree(p->d_thalf);
+    delete p;
+}
+
+Plan *plan_of(const void *vp) {
+    if (!vp) return nullptr;
+    // both precisions share the layout up to ext_fftm_obj
+    const vsip_fftm_f *f = (const vsip_fftm_f *)vp;
+    return (Plan *)f->ext_fftm_obj;
+}
+
+template <typename VP, typename T>
+static VP *create(int type, vsip_length M, vsip_length N, double scale, int dir, vsip_major major,
+                  unsigned ntimes, vsip_alg_hint hint) {
+    if (!device()) return NULL;
+    VP *vp = (VP *)calloc(1, sizeof(VP));
+    if (!vp) {
+        set_error(E_ALLOC, "plan allocation");
+        return NULL;
+    }
+    Plan *p = new (std::nothrow) Plan();
+    if (!p) {
+        free(vp);
+        set_error(E_ALLOC, "plan allocation");
+        return NULL;
+    }
+    p->type = type;
+    p->prec = sizeof(T) == 4 ? P_F32 : P_F64;
+    p->M = (long)M;
+    p->N = (long)N;
+    p->major = (major == VSIP_COL) ? 1 : 0;
+    if (type == JV_RCFFTOP || type == JV_CRFFTOP) {
+        p->MN = (long)(p->major == 0 ? N / 2 : M / 2);
+        p->mN = (long)(p->major == 0 ? M : N);
+        p->dir = (type == JV_RCFFTOP) ? -1 : 1;
+    } else {
+        p->MN = (long)(p->major == 1 ? M : N);
+        p->mN = (long)(p->major == 1 ? N : M);
+        p->dir = dir;
+    }
+    p->scale = scale;
+    p->ntimes = ntimes;
+    p->hint = (int)hint;
+    p->radix = pass_radices(p->MN, &p->smooth);
+    unsigned long pn[8], p0[8], pF[8];
+    unsigned long ns = ref_factor((unsigned long)p->MN, pn, p0, pF);
+    if (ns > 0) {
+        p->jofk.resize(p->MN);
+        for (long i = 0; i < p->MN; i++) p->jofk[i] = ref_jofk((unsigned long)i, pn, p0, pF[ns - 1], ns);
+    }
+    if (!make_tables<T>(p)) {
+        plan_free(p);
+        free(vp);
+        return NULL;
+    }
+    // attributes with the reference's meaning (c_VSIP_src/vsip_fftmattributes_f.h)
+    vp->scale = (T)scale;
+    vp->N = N;
+    vp->M = M;
+    vp->MN = (vsip_length)p->MN;
+    vp->mN = (vsip_length)p->mN;
+    vp->major = major;
+    vp->length = ns;
+    vp->d = (vsip_fft_dir)p->dir;
+    vp->type = type;
+    vp->dft = (ns > 0 && p0[0] == 1 && pF[0] == (unsigned long)p->MN) ? 1 : 0;
+    vp->ntimes = ntimes;
+    vp->hint = hint;
+    vp->ext_fftm_obj = p;
+    return vp;
+}
+
+template <typename VP>
+static int destroy(VP *vp) {
+    if (vp) {
+        plan_free((Plan *)vp->ext_fftm_obj);
+        free(vp);
+    }
+    return 0;
+}
+
+template <typename VP, typename A>
+static void getattr(const VP *fft, A *attr) {
+    // c_VSIP_src/vsip_fftm_getattr_f.c:18-69
+    if (!fft || !attr) return;
+    attr->input.r = fft->M;
+    attr->input.c = fft->N;
+    attr->output.r = fft->M;
+    attr->output.c = fft->N;
+    attr->place = VSIP_FFT_OP;
+    switch (fft->type) {
+        case JV_CCFFTIP: attr->place = VSIP_FFT_IP; break;
+        case JV_RCFFTOP:
+            attr->output.r = (fft->major == VSIP_ROW) ? fft->mN : (fft->MN + 1);
+            attr->output.c = (fft->major == VSIP_ROW) ? (fft->MN + 1) : fft->mN;
+            break;
+        case JV_CRFFTOP:
+            attr->input.r = (fft->major == VSIP_ROW) ? fft->mN : (fft->MN + 1);
+            attr->input.c = (fft->major == VSIP_ROW) ? (fft->MN + 1) : fft->mN;
+            break;
+        default: break;
+    }
+    attr->dir = fft->d;
+    attr->scale = fft->scale;
+    attr->major = fft->major;
+}
+
+}  // namespace jv
+
+using namespace jv;
+
+extern "C" {
+
+vsip_fftm_f *vsip_ccfftmop_create_f(vsip_length M, vsip_length N, vsip_scalar_f scale, vsip_fft_dir dir,
+                                    vsip_major major, unsigned int ntimes, vsip_alg_hint hint) {
+    return create<vsip_fftm_f, float>(JV_CCFFTOP, M, N, scale, dir, major, ntimes, hint);
+}
+vsip_fftm_f *vsip_ccfftmip_create_f(vsip_length M, vsip_length N, vsip_scalar_f scale, vsip_fft_dir dir,
+                                    vsip_major major, unsigned int ntimes, vsip_alg_hint hint) {
+    return create<vsip_fftm_f, float>(JV_CCFFTIP, M, N, scale, dir, major, ntimes, hint);
+}
+vsip_fftm_f *vsip_rcfftmop_create_f(vsip_length M, vsip_length N, vsip_scalar_f scale, vsip_major major,
+                                    unsigned int ntimes, vsip_alg_hint hint) {
+    return create<vsip_fftm_f, float>(JV_RCFFTOP, M, N, scale, VSIP_FFT_FWD, major, ntimes, hint);
+}
+vsip_fftm_f *vsip_crfftmop_create_f(vsip_length M, vsip_length N, vsip_scalar_f scale, vsip_major major,
+                                    unsigned int ntimes, vsip_alg_hint hint) {
+    return create<vsip_fftm_f, float>(JV_CRFFTOP, M, N, scale, VSIP_FFT_INV, major, ntimes, hint);
+}
+vsip_fftm_d *vsip_ccfftmop_create_d(vsip_length M, vsip_length N, vsip_scalar_d scale, vsip_fft_dir dir,
+                                    vsip_major major, unsigned int ntimes, vsip_alg_hint hint) {
+    return create<vsip_fftm_d, double>(JV_CCFFTOP, M, N, scale, dir, major, ntimes, hint);
+}
+vsip_fftm_d *vsip_ccfftmip_create_d(vsip_length M, vsip_length N, vsip_scalar_d scale, vsip_fft_dir dir,
+                                    vsip_major major, unsigned int ntimes, vsip_alg_hint hint) {
+    return create<vsip_fftm_d, double>(JV_CCFFTIP, M, N, scale, dir, major, ntimes, hint);
+}
+vsip_fftm_d *vsip_rcfftmop_create_d(vsip_length M, vsip_length N, vsip_scalar_d scale, vsip_major major,
+                                    unsigned int ntimes, vsip_alg_hint hint) {
+    return create<vsip_fftm_d, double>(JV_RCFFTOP, M, N, scale, VSIP_FFT_FWD, major, ntimes, hint);
+}
+vsip_fftm_d *vsip_crfftmop_create_d(vsip_length M, vsip_length N, vsip_scalar_d scale, vsip_major major,
+                                    unsigned int ntimes, vsip_alg_hint hint) {
+    return create<vsip_fftm_d, double>(JV_CRFFTOP, M, N, scale, VSIP_FFT_INV, major, ntimes, hint);
+}
+
+int vsip_fftm_destroy_f(vsip_fftm_f *p) { return destroy(p); }
+int vsip_fftm_destroy_d(vsip_fftm_d *p) { return destroy(p); }
+void vsip_fftm_getattr_f(const vsip_fftm_f *p, vsip_fftm_attr_f *a) { getattr(p, a); }
+void vsip_fftm_getattr_d(const vsip_fftm_d *p, vsip_fftm_attr_d *a) { getattr(p, a); }
+
+int jvsip_fftm_setform_f(vsip_fftm_f *vp, int form) {
+    Plan *p = plan_of(vp);
+    if (!p || form < JVSIP_FORM_AUTO || form > JVSIP_FORM_SPLIT_FP16) return E_ARG;
+    p->form = form;
+    return 0;
+}
+int jvsip_fftm_getform_f(const vsip_fftm_f *vp) {
+    Plan *p = plan_of(vp);
+    return p ? p->form : -1;
+}
+
+// Plan introspection for tests and tools: the device pass radices and the
+// reference digit-reversal map.  Returns the count written (or needed).
+int jvsip_fftm_passes(const void *vp, int *radix, int cap) {
+    Plan *p = plan_of(vp);
+    if (!p) return -1;
+    int n = (int)p->radix.size();
+    for (int i = 0; i < n && i < cap; i++) radix[i] = p->radix[i];
+    return n;
+}
+long jvsip_fftm_jofk(const void *vp, unsigned long *out, long cap) {
+    Plan *p = plan_of(vp);
+    if (!p) return -1;
+    long n = (long)p->jofk.size();
+    for (long i = 0; i < n && i < cap; i++) out[i] = p->jofk[i];
+    return n;
+}
+
+}  // extern "C"

@@ -1,0 +1,76 @@
+"""GPU parity: every golden case through the C ABI of the GPU library, in the
+host-staged mode (blocks not admitted) and the device-resident mode (blocks
+admitted to device mirrors), against the reference's outputs within
+rel-L2 <= 1e-6*log2(N) (_f) / 1e-14*log2(N) (_d); elements outside the output
+view must be left untouched; and the reference's own known-answer tests."""
+import numpy as np
+import pytest
+
+import golden_cases as G
+import gpu_run as R
+import jvsip_gb300 as J
+import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("admit", [False, True], ids=["staged", "resident"])
+@pytest.mark.parametrize("case", G.cases(), ids=lambda c: c["id"])
+def test_golden_case(case, admit):
+    out, before = R.run_case_gpu(case, admit)
+    idx, ref = G.reference_values(case)
+    err = G.rel_l2(out[idx], ref)
+    assert err <= R.tolerance(case), f"rel-L2 {err:.3e} > {R.tolerance(case):.3e}"
+    mask = R.view_mask(case)
+    # nothing outside the output view may change
+    assert np.array_equal(out[~mask], before[~mask])
+
+
+@pytest.mark.parametrize("tc", G.ref_tests(), ids=lambda t: f"{t['file'].split('/')[-1]}:{t['line']}")
+def test_reference_known_answer(tc):
+    dtype = np.float32 if tc["prec"] == "f" else np.float64
+    o, cs, cl, rs, rl = tc["bind"]
+    x = O.CView(np.zeros(2 * tc["block"], dtype), o, cs, cl, rs, rl)
+    x.set(np.array(tc["x_re"]).reshape(cl, rl) + 1j * np.array(tc["x_im"]).reshape(cl, rl))
+    gold = np.array(tc["gold_re"]).reshape(cl, rl) + 1j * np.array(tc["gold_im"]).reshape(cl, rl)
+    kind = J.KIND_CCOP if tc["kind"] == "ccop" else J.KIND_CCIP
+    p = J.FFTM(kind, tc["M"], tc["N"], tc["scale"], tc["dir"], tc["major"], dtype)
+    bx = J.CBlock(x.buf)
+    vx = bx.view(o, cs, cl, rs, rl)
+    if kind == J.KIND_CCOP:
+        y = O.dense_cview(tc["M"], tc["N"], dtype)
+        by = J.CBlock(y.buf)
+        vy = by.view(0, tc["N"], tc["M"], 1, tc["N"])
+        p.ccfftmop(vx, vy)
+        got = y.get()
+    else:
+        p.ccfftmip(vx)
+        got = x.get()
+    assert float(np.mean(np.abs(got - gold) ** 2)) < tc["tol_meansq"]
+
+
+def test_plan_attributes_and_schedule():
+    p = J.FFTM(J.KIND_RCOP, 4096, 1536, 1.0, J.VSIP_FFT_FWD, J.VSIP_ROW)
+    a = p.getattr()
+    assert (a.input.r, a.input.c, a.output.r, a.output.c) == (4096, 1536, 4096, 769)
+    assert a.place == 1 and a.dir == -1 and a.major == 0
+    q = J.FFTM(J.KIND_CCIP, 1000, 4096, 0.5, J.VSIP_FFT_INV, J.VSIP_COL)
+    a = q.getattr()
+    assert a.place == 0 and a.dir == 1 and a.major == 1 and abs(a.scale - 0.5) < 1e-7
+    assert int(np.prod(q.passes())) == 1000
+    assert q.jofk(1000) == O.jofk(1000)
+
+
+def test_caller_quirk_scale_minus_one():
+    # example21.c / kw.c pass (..., VSIP_FFT_FWD, 1, VSIP_COL, ...) to ccfftmip_create:
+    # scale = -1 and dir = +1; the result must be the inverse transform times -1.
+    M, N = 16, 3
+    x = O.dense_cview(M, N)
+    x.buf[:] = O.fill(x.buf.size, 9, 0)
+    p = J.FFTM(J.KIND_CCIP, M, N, -1.0, 1, J.VSIP_COL)
+    o = O.Plan(O.CCIP, M, N, -1.0, 1, O.COL)
+    xo = O.CView(x.buf.copy(), 0, N, M, 1, N)
+    o.ccfftmip(xo)
+    b = J.CBlock(x.buf)
+    p.ccfftmip(b.view(0, N, M, 1, N))
+    assert G.rel_l2(x.buf, xo.buf) < 1e-6 * 4
