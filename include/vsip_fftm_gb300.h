@@ -272,6 +272,8 @@ int jvsip_gpu_synchronize(void);
 /* The CUDA stream (cudaStream_t, as void*) all of this library's device work
  * is ordered on; callers may record events on it or make their streams wait. */
 void *jvsip_gpu_stream(void);
+/* Number of kernels this library has launched since it was loaded. */
+unsigned long jvsip_gpu_kernel_launches(void);
 /* Plan introspection: the device pass radices (returns their count) and the
  * reference's digit-reversal map of the plan length (c_VSIP_src/VI_jofk.h),
  * kept for parity checks (returns the map length). */

@@ -12,6 +12,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <atomic>
 #include <map>
 #include <unordered_map>
 #include <unordered_set>
@@ -71,6 +72,10 @@ Device *device() {
     g_dev = d;
     return &g_dev;
 }
+
+// ------------------------------------------------------------------ launch counter
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 // ------------------------------------------------------------------ memory pool
 static std::mutex g_pool_mu;
@@ -527,3 +532,6 @@ extern "C" void *jvsip_gpu_stream(void) {
     Device *d = device();
     return d ? (void *)d->stream : nullptr;
 }
+
+// Number of kernels this library has launched since it was loaded.
+extern "C" unsigned long jvsip_gpu_kernel_launches(void) { return (unsigned long)g_launches.load(); }

@@ -40,6 +40,9 @@ struct Device {
 };
 Device *device();   // lazily initialised; nullptr (and error recorded) when no GPU
 
+// Kernel launches issued by this library (all kernels), for tools and benchmarks.
+void count_launch(unsigned n = 1);
+
 // ------------------------------------------------------------------ memory pool
 // Caching device allocator: freed buffers are kept per exact size class and
 // reused, so repeated calls do not cudaMalloc.  Thread-safe.

@@ -120,6 +120,7 @@ static bool launch_smem_v(SmemArgs<T> &a, const Job &j, long vpb, long ld, cudaS
         return false;
     }
     k_smem<T, EMAX, MAXT><<<(unsigned)grid, (unsigned)nthr, smem, st>>>(a);
+    count_launch();
     return cuda_ok(cudaGetLastError(), "k_smem launch");
 }
 
@@ -209,6 +210,7 @@ static bool gpass(const GPassArgs<T> &a, cudaStream_t st) {
     if (grid > gmax) grid = gmax;
     if (grid < 1) grid = 1;
     k_gpass<T><<<(unsigned)grid, 256, 0, st>>>(a);
+    count_launch();
     return cuda_ok(cudaGetLastError(), "k_gpass launch");
 }
 
@@ -334,6 +336,7 @@ bool launch_global_t(const Job &j, cudaStream_t st) {
             s.xout = csto<T>(j.cout);
             s.thalf = (const C *)j.thalf;
             k_r2c_split<T><<<grid_for<T>(j.nvec * (N + 1)), 256, 0, st>>>(s);
+            count_launch();
             ok = cuda_ok(cudaGetLastError(), "k_r2c_split launch");
         }
     } else {
@@ -345,6 +348,7 @@ bool launch_global_t(const Job &j, cudaStream_t st) {
         s.ydst = (C *)cur;
         s.thalf = (const C *)j.thalf;
         k_c2r_unsplit<T><<<grid_for<T>(j.nvec * N), 256, 0, st>>>(s);
+        count_launch();
         ok = cuda_ok(cudaGetLastError(), "k_c2r_unsplit launch");
         int Ns = 1;
         for (int p = 0; p < j.npass && ok; p++) {
@@ -369,6 +373,7 @@ bool launch_global_t(const Job &j, cudaStream_t st) {
             u.y = (const C *)cur;
             u.xout = rsto<T>(j.rout);
             k_c2r_unpack<T><<<grid_for<T>(j.nvec * N), 256, 0, st>>>(u);
+            count_launch();
             ok = cuda_ok(cudaGetLastError(), "k_c2r_unpack launch");
         }
     }
