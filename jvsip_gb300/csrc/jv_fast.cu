@@ -1,10 +1,203 @@
-// jv_fast.cu -- specialised register-resident kernels for the hot shapes.
-#include "jv_core.h"
+// jv_fast.cu -- register-resident kernels for contiguous rows (single
+// precision, interleaved, unit element stride, any row pitch).
+//
+// A transform of N = R1*R2*...*Rp points is held by T threads, E = N/T
+// complex values each, in registers.  Pass 1 reads global memory directly
+// (element t + T*b + r*N/R1: consecutive threads read consecutive elements),
+// the middle passes exchange through shared memory, and the last pass writes
+// global memory directly (element t + T*b + r*N/Rp, again coalesced): the
+// self-sorting Stockham order needs no digit-reversal pass, so every point is
+// read from and written to HBM exactly once.  Shared memory is indexed
+// i + (i >> 4), which makes every pass's stores and loads conflict-free for
+// 8-byte elements.  Several transforms share a CTA when N is small.
+#include <stdio.h>
+#include <stdlib.h>
+
+#include "jv_kernels.cuh"
 
 namespace jv {
-bool launch_fast_f32(const Job &j, cudaStream_t s) {
-    (void)j;
-    (void)s;
-    return false;
+
+template <int... Rs> struct RList;
+template <int R0, int... Rs> struct RList<R0, Rs...> {
+    static constexpr int first = R0;
+    typedef RList<Rs...> rest;
+};
+template <> struct RList<> {};
+
+__device__ __forceinline__ int padx(int i) { return i + (i >> 4); }
+
+struct FastArgs {
+    const float2 *in;   // row v starts at in + off_in + v*vs_in
+    float2 *out;
+    long off_in, vs_in, off_out, vs_out;
+    long nvec;
+    int inv;
+    int has_scale;
+    float scale;
+    const float2 *tw;  // exp(-2 pi i m/N), m < N
+};
+
+// twiddle and DFT of the thread's E/R butterflies of a radix-R pass
+template <int N, int T, int R, int E>
+__device__ __forceinline__ void fast_bfly(float2 (&v)[E], int t, int Ns, const float2 *__restrict__ tw) {
+    constexpr int B = E / R;
+#pragma unroll
+    for (int b = 0; b < B; b++) {
+        if (Ns > 1) {
+            int j = t + T * b;
+            int m = j % Ns;
+            int st = m * (N / (Ns * R));
+#pragma unroll
+            for (int r = 1; r < R; r++) v[b * R + r] = cmul(v[b * R + r], __ldg(&tw[r * st]));
+        }
+        Dft<float2, R>::run(&v[b * R]);
+    }
 }
+
+template <int N, int T, int E, int R>
+__device__ __forceinline__ void load_pass(float2 (&v)[E], const float2 *s, int t) {
+    constexpr int B = E / R;
+#pragma unroll
+    for (int b = 0; b < B; b++)
+#pragma unroll
+        for (int r = 0; r < R; r++) v[b * R + r] = s[padx(t + T * b + r * (N / R))];
+}
+
+template <int N, int T, int E, int R>
+__device__ __forceinline__ void store_pass(const float2 (&v)[E], float2 *s, int t, int Ns) {
+    constexpr int B = E / R;
+#pragma unroll
+    for (int b = 0; b < B; b++) {
+        int j = t + T * b;
+        int m = j % Ns;
+        int base = (j - m) * R + m;
+#pragma unroll
+        for (int r = 0; r < R; r++) s[padx(base + r * Ns)] = v[b * R + r];
+    }
+}
+
+// Passes after the first.  On entry shared memory holds the previous pass's output.
+template <int N, int T, int E, int NsIn, typename L> struct Passes;
+
+template <int N, int T, int E, int NsIn, int R0, int... Rs> struct Passes<N, T, E, NsIn, RList<R0, Rs...>> {
+    static __device__ __forceinline__ void run(float2 (&v)[E], float2 *s, int t, const FastArgs &a, long row,
+                                               bool live) {
+        __syncthreads();
+        load_pass<N, T, E, R0>(v, s, t);
+        fast_bfly<N, T, R0, E>(v, t, NsIn, a.tw);
+        if constexpr (sizeof...(Rs) == 0) {
+            // last pass: j < N/R0 = NsIn, so element j + r*NsIn -- coalesced stores
+            if (live) {
+                float2 *o = a.out + a.off_out + row * a.vs_out;
+                constexpr int B = E / R0;
+#pragma unroll
+                for (int b = 0; b < B; b++) {
+                    int j = t + T * b;
+#pragma unroll
+                    for (int r = 0; r < R0; r++) {
+                        float2 c = v[b * R0 + r];
+                        if (a.inv) c.y = -c.y;
+                        if (a.has_scale) c = cscale(c, a.scale);
+                        o[j + r * NsIn] = c;
+                    }
+                }
+            }
+        } else {
+            __syncthreads();
+            store_pass<N, T, E, R0>(v, s, t, NsIn);
+            Passes<N, T, E, NsIn * R0, RList<Rs...>>::run(v, s, t, a, row, live);
+        }
+    }
+};
+
+template <int N, int T, int RPC, typename L>
+__global__ void __launch_bounds__(T *RPC) k_fast(const FastArgs pa) {
+    constexpr int E = N / T;
+    constexpr int R1 = L::first;
+    constexpr int NP = N + N / 16;  // padded row in shared memory
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const FastArgs a = pa;
+    const int t = threadIdx.x % T;
+    const int rl = threadIdx.x / T;
+    const long row = (long)blockIdx.x * RPC + rl;
+    float2 *s = reinterpret_cast<float2 *>(smem_raw) + rl * NP;
+    // rows past the end (last CTA only) recompute the last row and store nothing,
+    // so every thread reaches every barrier
+    const bool live = row < a.nvec;
+    const long rowc = live ? row : a.nvec - 1;
+    float2 v[E];
+    const float2 *in = a.in + a.off_in + rowc * a.vs_in;
+    constexpr int B1 = E / R1;
+#pragma unroll
+    for (int b = 0; b < B1; b++)
+#pragma unroll
+        for (int r = 0; r < R1; r++) {
+            float2 c = in[t + T * b + r * (N / R1)];
+            if (a.inv) c.y = -c.y;
+            v[b * R1 + r] = c;
+        }
+    fast_bfly<N, T, R1, E>(v, t, 1, a.tw);
+    store_pass<N, T, E, R1>(v, s, t, 1);
+    Passes<N, T, E, R1, typename L::rest>::run(v, s, t, a, rowc, live);
+}
+
+template <int N, int T, int RPC, typename L>
+static bool launch_fast_n(const Job &j, cudaStream_t st) {
+    FastArgs a;
+    a.in = (const float2 *)j.cin.re;
+    a.out = (float2 *)j.cout.re;
+    a.off_in = j.cin.off;
+    a.vs_in = j.cin.vs;
+    a.off_out = j.cout.off;
+    a.vs_out = j.cout.vs;
+    a.nvec = j.nvec;
+    a.inv = j.inv;
+    a.has_scale = j.has_scale;
+    a.scale = (float)j.scale;
+    a.tw = (const float2 *)j.tw;
+    constexpr int NP = N + N / 16;
+    size_t smem = (size_t)RPC * NP * sizeof(float2);
+    static bool attr = false;
+    if (!attr) {
+        if (smem > 48 * 1024 &&
+            !cuda_ok(cudaFuncSetAttribute(k_fast<N, T, RPC, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem),
+                     "cudaFuncSetAttribute"))
+            return false;
+        attr = true;
+    }
+    long grid = (j.nvec + RPC - 1) / RPC;
+    k_fast<N, T, RPC, L><<<(unsigned)grid, T * RPC, smem, st>>>(a);
+    count_launch();
+    return cuda_ok(cudaGetLastError(), "k_fast launch");
+}
+
+// Specialised kernels: contiguous interleaved rows, any pitch, forward or
+// inverse (conjugation folded into load and store), optional scale.
+bool launch_fast_f32(const Job &j, cudaStream_t st) {
+    if (getenv("JVSIP_GPU_NO_FAST")) return false;
+    if (j.kind != K_C2C || j.prec != P_F32) return false;
+    const CView &ci = j.cin, &co = j.cout;
+    // interleaved, unit element stride, 8-byte aligned, rows of the transform contiguous
+    if (ci.cst != 2 || co.cst != 2 || ci.es != 1 || co.es != 1) return false;
+    if ((const float *)ci.im != (const float *)ci.re + 1 || (const float *)co.im != (const float *)co.re + 1)
+        return false;
+    if (((uintptr_t)ci.re % 8) || ((uintptr_t)co.re % 8)) return false;
+    if (j.nvec <= 0 || j.nvec > 0x7fffffffL * 1L) return false;
+    // rows of an in-place call must not overlap each other (each CTA reads its
+    // rows completely before it writes them)
+    if (j.nvec > 1 && (labs(ci.vs) < j.N || labs(co.vs) < j.N)) return false;
+    switch (j.N) {
+        case 64: return launch_fast_n<64, 4, 64, RList<16, 4>>(j, st);
+        case 128: return launch_fast_n<128, 8, 32, RList<16, 8>>(j, st);
+        case 256: return launch_fast_n<256, 16, 16, RList<16, 16>>(j, st);
+        case 512: return launch_fast_n<512, 32, 8, RList<16, 16, 2>>(j, st);
+        case 1024: return launch_fast_n<1024, 64, 4, RList<16, 16, 4>>(j, st);
+        case 2048: return launch_fast_n<2048, 128, 2, RList<16, 16, 8>>(j, st);
+        case 4096: return launch_fast_n<4096, 256, 1, RList<16, 16, 16>>(j, st);
+        case 8192: return launch_fast_n<8192, 512, 1, RList<16, 16, 16, 2>>(j, st);
+        default: return false;
+    }
+}
+
 }  // namespace jv

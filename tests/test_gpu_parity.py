@@ -74,3 +74,17 @@ def test_caller_quirk_scale_minus_one():
     b = J.CBlock(x.buf)
     p.ccfftmip(b.view(0, N, M, 1, N))
     assert G.rel_l2(x.buf, xo.buf) < 1e-6 * 4
+
+
+GENERIC_IDS = {"cfg1_f_fwd", "cfg1_f_inv", "cfg3_f_fwd", "cfg3_f_inv_ip", "len64_f", "len128_f", "len256_f",
+               "len512_f", "len1024_f", "len2048_f", "len4096_f", "len8192_f", "cfg4_f", "alias_f"}
+
+
+@pytest.mark.parametrize("case", [c for c in G.cases() if c["id"] in GENERIC_IDS], ids=lambda c: c["id"])
+def test_generic_kernel_on_fast_shapes(case, monkeypatch):
+    # the specialised row kernels take these shapes by default; check the
+    # general shared-memory kernel on them too
+    monkeypatch.setenv("JVSIP_GPU_NO_FAST", "1")
+    out, before = R.run_case_gpu(case, True)
+    idx, ref = G.reference_values(case)
+    assert G.rel_l2(out[idx], ref) <= R.tolerance(case)
