@@ -69,6 +69,8 @@ Device *device() {
         !cuda_ok(cudaStreamCreateWithFlags(&d.h2d, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !cuda_ok(cudaStreamCreateWithFlags(&d.d2h, cudaStreamNonBlocking), "cudaStreamCreate"))
         return nullptr;
+    for (int i = 0; i < 128; i++)
+        if (!cuda_ok(cudaEventCreateWithFlags(&d.ev[i], cudaEventDisableTiming), "cudaEventCreate")) return nullptr;
     g_dev = d;
     return &g_dev;
 }

@@ -37,6 +37,7 @@ struct Device {
     cudaStream_t stream = nullptr;  // library stream (all device work is ordered on it)
     cudaStream_t h2d = nullptr;     // staging copy streams for host-resident views
     cudaStream_t d2h = nullptr;
+    cudaEvent_t ev[128];            // chunk events of the pipelined staging path
 };
 Device *device();   // lazily initialised; nullptr (and error recorded) when no GPU
 
@@ -99,6 +100,7 @@ struct Job {
     int inplace = 0;     // input and output are the same storage
     const void *tw = nullptr;     // forward table exp(-2 pi i m/N), m < N, dtype complex
     const void *thalf = nullptr;  // R2C/C2R table exp(-+ i pi k/MN), k <= MN
+    const void *twp = nullptr;    // per-pass twiddle tables of the specialised kernel (or null)
     int npass = 0;
     int radix[40];
 };
@@ -109,6 +111,7 @@ bool launch_smem_f64(const Job &j, cudaStream_t s);
 bool launch_global_f32(const Job &j, cudaStream_t s);
 bool launch_global_f64(const Job &j, cudaStream_t s);
 bool launch_fast_f32(const Job &j, cudaStream_t s);   // specialised kernels; false when none fits
+std::vector<int> fast_radices(long N);                // radix list of the specialised kernel for N
 
 // Capacity queries used by the dispatcher.
 long smem_max_len(int prec, int kind);   // largest N the shared-memory kernel takes
@@ -128,6 +131,7 @@ struct Plan {
     bool smooth = true;       // every radix is one of the built-in codelets
     void *d_tw = nullptr;     // forward twiddles, MN entries
     void *d_thalf = nullptr;  // half-angle table, MN+1 entries (real transforms)
+    void *d_twp = nullptr;    // per-pass [r][m] twiddle tables of the specialised kernel
     std::vector<unsigned long> jofk;  // reference digit-reversal map (kept for parity checks)
     std::mutex mu;            // the plan is used by one call at a time
 };

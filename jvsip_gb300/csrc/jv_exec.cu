@@ -25,6 +25,8 @@ long smem_max_len_f64(int kind);
 
 long smem_max_len(int prec, int kind) { return prec == P_F32 ? smem_max_len_f32(kind) : smem_max_len_f64(kind); }
 
+static bool run_job(Job &j, cudaStream_t st);
+
 // ---------------------------------------------------------------- staging of host blocks
 // One staged region: scalars [lo*cst, (hi+1)*cst) of a host array (and of its
 // imaginary array for split blocks) copied to one device buffer.
@@ -277,8 +279,89 @@ static void fill_job(Job &j, const Plan *p, int kind) {
     j.scale = p->scale;
     j.tw = p->d_tw;
     j.thalf = p->d_thalf;
+    j.twp = p->d_twp;
     j.npass = (int)p->radix.size();
     for (int i = 0; i < j.npass && i < 40; i++) j.radix[i] = p->radix[i];
+}
+
+// Host-resident c2c call whose views are rows of unit element stride and
+// positive pitch (the common dense case): the transforms are cut into chunks
+// that flow host -> device (copy stream), kernel (library stream), device ->
+// host (second copy stream), so both copy directions and the kernels overlap.
+// Each chunk is copied with a 2-D copy of exactly its rows, so pitched views
+// need no read-back of the gaps.  Returns false (nothing done) when the views
+// do not qualify.
+template <typename T, typename CB>
+static bool pipelined_cc(Job &j, const CRes<T, CB> &rx, const CRes<T, CB> &ry, bool same_view, bool *ok) {
+    if (getenv("JVSIP_GPU_NO_PIPELINE")) return false;
+    if (rx.m || ry.m) return false;
+    if (rx.blk->cstride != 2 || ry.blk->cstride != 2) return false;
+    const long len = j.N, nv = j.nvec;
+    if (rx.g.es != 1 || ry.g.es != 1 || rx.g.vs < len || ry.g.vs < len || nv < 2) return false;
+    if (!same_view && rx.blk == ry.blk) return false;  // overlapping spans are handled by the general path
+    const size_t esz = 2 * sizeof(T);
+    const size_t row_b = (size_t)len * esz;
+    const size_t total = row_b * (size_t)nv;
+    if (total < ((size_t)64 << 20)) return false;       // small calls: one copy each way is as good
+    Device *d = device();
+    long chunks = (long)(total / ((size_t)128 << 20));
+    if (chunks < 4) chunks = 4;
+    if (chunks > 32) chunks = 32;
+    if (chunks > nv) chunks = nv;
+    const long rpc = (nv + chunks - 1) / chunks;
+    chunks = (nv + rpc - 1) / rpc;
+    char *din = (char *)dmalloc(total);
+    char *dout = same_view ? din : (char *)dmalloc(total);
+    if (!din || !dout) {
+        dfree(din);
+        if (!same_view) dfree(dout);
+        *ok = false;
+        return true;
+    }
+    const char *hx = (const char *)rx.blk->R->array + (size_t)rx.g.off * esz;
+    char *hy = (char *)ry.blk->R->array + (size_t)ry.g.off * esz;
+    bool good = true;
+    // the copy-in of a chunk must not overtake earlier library work that may
+    // still read the pool buffers it reuses
+    cudaEvent_t *ev = d->ev;
+    good = good && cuda_ok(cudaEventRecord(ev[0], d->stream), "event");
+    good = good && cuda_ok(cudaStreamWaitEvent(d->h2d, ev[0], 0), "wait");
+    for (long c = 0; c < chunks && good; c++) {
+        long r0 = c * rpc, r1 = std::min(nv, r0 + rpc);
+        cudaEvent_t ein = ev[1 + 2 * (c % 63)], eker = ev[2 + 2 * (c % 63)];
+        good = cuda_ok(cudaMemcpy2DAsync(din + (size_t)r0 * row_b, row_b, hx + (size_t)r0 * rx.g.vs * esz,
+                                         (size_t)rx.g.vs * esz, row_b, (size_t)(r1 - r0), cudaMemcpyHostToDevice,
+                                         d->h2d), "pipelined copy in");
+        good = good && cuda_ok(cudaEventRecord(ein, d->h2d), "event");
+        good = good && cuda_ok(cudaStreamWaitEvent(d->stream, ein, 0), "wait");
+        Job q = j;
+        q.nvec = r1 - r0;
+        q.cin.re = din + (size_t)r0 * row_b;
+        q.cin.im = (T *)q.cin.re + 1;
+        q.cin.cst = 2;
+        q.cin.off = 0;
+        q.cin.es = 1;
+        q.cin.vs = len;
+        q.cout = q.cin;
+        q.cout.re = dout + (size_t)r0 * row_b;
+        q.cout.im = (T *)q.cout.re + 1;
+        q.inplace = same_view ? 1 : 0;
+        good = good && run_job(q, d->stream);
+        good = good && cuda_ok(cudaEventRecord(eker, d->stream), "event");
+        good = good && cuda_ok(cudaStreamWaitEvent(d->d2h, eker, 0), "wait");
+        good = good && cuda_ok(cudaMemcpy2DAsync(hy + (size_t)r0 * ry.g.vs * esz, (size_t)ry.g.vs * esz,
+                                                 dout + (size_t)r0 * row_b, row_b, row_b, (size_t)(r1 - r0),
+                                                 cudaMemcpyDeviceToHost, d->d2h), "pipelined copy out");
+    }
+    // later library work is ordered after the copy-out, then wait for it
+    cuda_ok(cudaEventRecord(ev[127], d->d2h), "event");
+    cuda_ok(cudaStreamWaitEvent(d->stream, ev[127], 0), "wait");
+    good = cuda_ok(cudaStreamSynchronize(d->d2h), "pipelined fftm") && good;
+    good = cuda_ok(cudaStreamSynchronize(d->stream), "pipelined fftm") && good;
+    dfree(din);
+    if (!same_view) dfree(dout);
+    *ok = good;
+    return true;
 }
 
 template <typename T, typename VP, typename CMV, typename CB>
@@ -307,6 +390,10 @@ static void exec_cc(const VP *vp, const CMV *x, const CMV *y, bool ip) {
     if (!ip) {
         ry = CRes<T, CB>{y->block, cgeo(y, p->major, p->MN, p->mN), mirror_find(y->block)};
         same_view = (x->block == y->block && rx.g.off == ry.g.off && rx.g.es == ry.g.es && rx.g.vs == ry.g.vs);
+    }
+    {
+        bool pok = false;
+        if (pipelined_cc<T, CB>(j, rx, ry, same_view, &pok)) return;
     }
     Staging stg;
     cudaStream_t st = d->stream;

@@ -13,6 +13,8 @@
 #include <stdio.h>
 #include <stdlib.h>
 
+#include <vector>
+
 #include "jv_kernels.cuh"
 
 namespace jv {
@@ -34,21 +36,21 @@ struct FastArgs {
     int inv;
     int has_scale;
     float scale;
-    const float2 *tw;  // exp(-2 pi i m/N), m < N
+    const float2 *twp; // per-pass twiddles: pass p at its offset, entry r*Ns + m = exp(-2 pi i r m/(Ns R))
 };
 
-// twiddle and DFT of the thread's E/R butterflies of a radix-R pass
-template <int N, int T, int R, int E>
-__device__ __forceinline__ void fast_bfly(float2 (&v)[E], int t, int Ns, const float2 *__restrict__ tw) {
+// twiddle and DFT of the thread's E/R butterflies of a radix-R pass; the
+// pass's twiddle table is laid out [r][m] so a warp's loads are contiguous
+template <int N, int T, int R, int E, int Ns>
+__device__ __forceinline__ void fast_bfly(float2 (&v)[E], int t, const float2 *__restrict__ tp) {
     constexpr int B = E / R;
 #pragma unroll
     for (int b = 0; b < B; b++) {
-        if (Ns > 1) {
+        if constexpr (Ns > 1) {
             int j = t + T * b;
             int m = j % Ns;
-            int st = m * (N / (Ns * R));
 #pragma unroll
-            for (int r = 1; r < R; r++) v[b * R + r] = cmul(v[b * R + r], __ldg(&tw[r * st]));
+            for (int r = 1; r < R; r++) v[b * R + r] = cmul(v[b * R + r], __ldg(&tp[r * Ns + m]));
         }
         Dft<float2, R>::run(&v[b * R]);
     }
@@ -77,14 +79,15 @@ __device__ __forceinline__ void store_pass(const float2 (&v)[E], float2 *s, int 
 }
 
 // Passes after the first.  On entry shared memory holds the previous pass's output.
-template <int N, int T, int E, int NsIn, typename L> struct Passes;
+template <int N, int T, int E, int NsIn, int Off, typename L> struct Passes;
 
-template <int N, int T, int E, int NsIn, int R0, int... Rs> struct Passes<N, T, E, NsIn, RList<R0, Rs...>> {
+template <int N, int T, int E, int NsIn, int Off, int R0, int... Rs>
+struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>> {
     static __device__ __forceinline__ void run(float2 (&v)[E], float2 *s, int t, const FastArgs &a, long row,
                                                bool live) {
         __syncthreads();
         load_pass<N, T, E, R0>(v, s, t);
-        fast_bfly<N, T, R0, E>(v, t, NsIn, a.tw);
+        fast_bfly<N, T, R0, E, NsIn>(v, t, a.twp + Off);
         if constexpr (sizeof...(Rs) == 0) {
             // last pass: j < N/R0 = NsIn, so element j + r*NsIn -- coalesced stores
             if (live) {
@@ -105,7 +108,7 @@ template <int N, int T, int E, int NsIn, int R0, int... Rs> struct Passes<N, T, 
         } else {
             __syncthreads();
             store_pass<N, T, E, R0>(v, s, t, NsIn);
-            Passes<N, T, E, NsIn * R0, RList<Rs...>>::run(v, s, t, a, row, live);
+            Passes<N, T, E, NsIn * R0, Off + R0 * NsIn, RList<Rs...>>::run(v, s, t, a, row, live);
         }
     }
 };
@@ -136,9 +139,9 @@ __global__ void __launch_bounds__(T *RPC) k_fast(const FastArgs pa) {
             if (a.inv) c.y = -c.y;
             v[b * R1 + r] = c;
         }
-    fast_bfly<N, T, R1, E>(v, t, 1, a.tw);
+    fast_bfly<N, T, R1, E, 1>(v, t, nullptr);
     store_pass<N, T, E, R1>(v, s, t, 1);
-    Passes<N, T, E, R1, typename L::rest>::run(v, s, t, a, rowc, live);
+    Passes<N, T, E, R1, R1, typename L::rest>::run(v, s, t, a, rowc, live);
 }
 
 template <int N, int T, int RPC, typename L>
@@ -154,7 +157,8 @@ static bool launch_fast_n(const Job &j, cudaStream_t st) {
     a.inv = j.inv;
     a.has_scale = j.has_scale;
     a.scale = (float)j.scale;
-    a.tw = (const float2 *)j.tw;
+    a.twp = (const float2 *)j.twp;
+    if (!a.twp) return false;
     constexpr int NP = N + N / 16;
     size_t smem = (size_t)RPC * NP * sizeof(float2);
     static bool attr = false;
@@ -170,6 +174,21 @@ static bool launch_fast_n(const Job &j, cudaStream_t st) {
     k_fast<N, T, RPC, L><<<(unsigned)grid, T * RPC, smem, st>>>(a);
     count_launch();
     return cuda_ok(cudaGetLastError(), "k_fast launch");
+}
+
+// Radix list of the specialised kernel for length N (empty: none).
+std::vector<int> fast_radices(long N) {
+    switch (N) {
+        case 64: return {16, 4};
+        case 128: return {16, 8};
+        case 256: return {16, 16};
+        case 512: return {16, 16, 2};
+        case 1024: return {16, 16, 4};
+        case 2048: return {16, 16, 8};
+        case 4096: return {16, 16, 16};
+        case 8192: return {16, 16, 16, 2};
+        default: return {};
+    }
 }
 
 // Specialised kernels: contiguous interleaved rows, any pitch, forward or

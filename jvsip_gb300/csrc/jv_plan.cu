@@ -128,6 +128,30 @@ static bool make_tables(Plan *p) {
     if (!p->d_tw) return false;
     if (!cuda_ok(cudaMemcpy(p->d_tw, tw.data(), 2 * n * sizeof(T), cudaMemcpyHostToDevice), "twiddle upload"))
         return false;
+    if (sizeof(T) == 4) {
+        // per-pass tables of the specialised kernel: pass with radix R after
+        // radices of product Ns holds exp(-2 pi i r m/(Ns R)) at r*Ns + m
+        std::vector<int> fr = fast_radices(MN);
+        if (!fr.empty()) {
+            std::vector<T> tp;
+            long Ns = 1;
+            for (int R : fr) {
+                for (long r = 0; r < R; r++)
+                    for (long m = 0; m < Ns; m++) {
+                        double c, s;
+                        unit_root((r * m) % (Ns * R), Ns * R, &c, &s);
+                        tp.push_back((T)c);
+                        tp.push_back((T)s);
+                    }
+                Ns *= R;
+            }
+            p->d_twp = dmalloc(tp.size() * sizeof(T));
+            if (!p->d_twp) return false;
+            if (!cuda_ok(cudaMemcpy(p->d_twp, tp.data(), tp.size() * sizeof(T), cudaMemcpyHostToDevice),
+                         "pass twiddle upload"))
+                return false;
+        }
+    }
     if (p->type == JV_RCFFTOP || p->type == JV_CRFFTOP) {
         // exp(-i pi k/MN) for R2C, exp(+i pi k/MN) for C2R, k = 0..MN
         // (c_VSIP_src/VI_rcfftmop_create_f_def.h:75-86, VI_crfftmop_create_f_def.h:72-83)
@@ -153,6 +177,7 @@ static void plan_free(Plan *p) {
     if (d) cudaStreamSynchronize(d->stream);
     dfree(p->d_tw);
     dfree(p->d_thalf);
+    dfree(p->d_twp);
     delete p;
 }
 
