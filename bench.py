@@ -315,14 +315,13 @@ def main():
     peak, peak_kind = peaks()
     kern_ms = statistics.mean(per)
     achieved = BYTES_PER_CALL / (kern_ms / 1e3) / 1e9
+    # DRAM bytes per launch from the committed ncu summary of this kernel (scaled by rows)
     traffic = None
-    tf = os.path.join(ROOT, "profiles", "traffic.json")
+    tf = os.path.join(ROOT, "profiles", "k_fast_c64_4096_rows.md")
     if os.path.exists(tf):
-        try:
-            with open(tf) as f:
-                traffic = json.load(f).get("ccfftmop_f_65536x4096_row", {}).get("bytes_per_launch")
-        except Exception:
-            traffic = None
+        for ln in open(tf):
+            if ln.startswith("traffic_bytes_per_launch_65536_rows:"):
+                traffic = int(int(ln.split(":")[1]) * M_ROWS / 65536)
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
