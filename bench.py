@@ -51,6 +51,8 @@ def args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--rows", type=int, default=M_ROWS, help="rows (smaller cases for profiling only)")
+    ap.add_argument("--workload", default="cfg3", choices=sorted(WORKLOADS),
+                    help="cfg3 (default headline) or another configuration, measured the same way")
     return ap.parse_args()
 
 
@@ -172,6 +174,142 @@ def reference_arm(a):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- other configurations
+# Each returns (plan, x_block, y_block, views, bytes_per_call, description, checker).
+WORKLOADS = {"cfg3": None, "cfg1": None, "cfg2rc": None, "cfg2cr": None, "cfg2col": None, "cfg3d": None,
+             "cfg4": None}
+
+
+def other_workload(a):
+    """Time one of the other configurations: GB/s of algorithmic bytes over --steps calls on
+    admitted blocks, with L2 flushed between calls when the data would fit in it."""
+    import numpy as np
+    import torch
+    import jvsip_gb300 as J
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    L = J.lib()
+    L.vsip_init(None)
+    ext = torch.cuda.ExternalStream(L.jvsip_gpu_stream())
+    w = a.workload
+    f32 = np.float32
+    if w == "cfg1":
+        M, N = 64, 1024
+        x = O.fill(2 * M * N, 1, 0, f32)
+        y = np.zeros_like(x)
+        plan = J.FFTM(J.KIND_CCOP, M, N, 1.0, -1, J.VSIP_ROW)
+        bx, by = J.CBlock(x), J.CBlock(y)
+        vx, vy = bx.view(0, N, M, 1, N), by.view(0, N, M, 1, N)
+        call = lambda: L.vsip_ccfftmop_f(plan.h, vx.h, vy.h)
+        nbytes, desc, dt = 16 * M * N, "vsip_ccfftmop_f 64x1024 c64 VSIP_ROW forward, U[-1,1)", "f32"
+        rows_check = ("row", M, N, x, y, np.float32, -1, 1.0, N)
+    elif w == "cfg2col":
+        M, N = 1000, 4096   # 1000-point transforms down 4096 columns of a row-major matrix
+        x = O.fill(2 * M * N, 3, 1, f32)
+        y = np.zeros_like(x)
+        plan = J.FFTM(J.KIND_CCOP, M, N, 1.0, -1, J.VSIP_COL)
+        bx, by = J.CBlock(x), J.CBlock(y)
+        vx, vy = bx.view(0, N, M, 1, N), by.view(0, N, M, 1, N)
+        call = lambda: L.vsip_ccfftmop_f(plan.h, vx.h, vy.h)
+        nbytes, desc, dt = 16 * M * N, "vsip_ccfftmop_f M=1000 x N=4096 c64 VSIP_COL forward, N(0,1)", "f32"
+        rows_check = ("col", M, N, x, y, np.float32, -1, 1.0, M)
+    elif w in ("cfg2rc", "cfg2cr"):
+        M, N, H = 4096, 1536, 769
+        xr = O.fill(M * N, 2, 1, f32)
+        z = np.zeros(2 * M * H, f32)
+        if w == "cfg2rc":
+            plan = J.FFTM(J.KIND_RCOP, M, N, 1.0, -1, J.VSIP_ROW)
+            bx, by = J.RBlock(xr), J.CBlock(z)
+            vx, vy = bx.view(0, N, M, 1, N), by.view(0, H, M, 1, H)
+            call = lambda: L.vsip_rcfftmop_f(plan.h, vx.h, vy.h)
+            desc = "vsip_rcfftmop_f 4096x1536 f32 -> 4096x769 c64 VSIP_ROW, N(0,1)"
+        else:
+            z[:] = O.fill(2 * M * H, 22, 1, f32)
+            plan = J.FFTM(J.KIND_CROP, M, N, 1.0 / N, 1, J.VSIP_ROW)
+            bx, by = J.CBlock(z), J.RBlock(xr)
+            vx, vy = bx.view(0, H, M, 1, H), by.view(0, N, M, 1, N)
+            call = lambda: L.vsip_crfftmop_f(plan.h, vx.h, vy.h)
+            desc = "vsip_crfftmop_f 4096x769 c64 -> 4096x1536 f32 VSIP_ROW, scale 1/1536"
+        nbytes, dt = M * (4 * N + 8 * H), "f32"
+        rows_check = None
+    elif w == "cfg3d":
+        M, N = 16384, 4096
+        x = np.empty(2 * M * N, np.float64)
+        g = torch.Generator(device="cuda").manual_seed(4)
+        x[:] = torch.randn(2 * M * N, device="cuda", dtype=torch.float64, generator=g).cpu().numpy()
+        y = np.zeros_like(x)
+        plan = J.FFTM(J.KIND_CCOP, M, N, 1.0, -1, J.VSIP_ROW, dtype=np.float64)
+        bx, by = J.CBlock(x), J.CBlock(y)
+        vx, vy = bx.view(0, N, M, 1, N), by.view(0, N, M, 1, N)
+        call = lambda: L.vsip_ccfftmop_d(plan.h, vx.h, vy.h)
+        nbytes, desc, dt = 32 * M * N, "vsip_ccfftmop_d 16384x4096 c128 VSIP_ROW forward, N(0,1)", "f64"
+        rows_check = ("row", M, N, x, y, np.float64, -1, 1.0, N)
+    elif w == "cfg4":
+        M, N = 32768, 1024
+        x = O.fill(2 * M * N, 5, 1, f32).reshape(M, 2 * N)
+        u = O.fill(M, 55, 0, np.float64) * 3.0
+        x *= (10.0 ** u).astype(f32)[:, None]
+        x = x.reshape(-1)
+        y = np.zeros_like(x)
+        plan = J.FFTM(J.KIND_CCOP, M, N, 1.0, -1, J.VSIP_ROW)
+        bx, by = J.CBlock(x), J.CBlock(y)
+        vx, vy = bx.view(0, N, M, 1, N), by.view(0, N, M, 1, N)
+        call = lambda: L.vsip_ccfftmop_f(plan.h, vx.h, vy.h)
+        nbytes, desc, dt = 16 * M * N, "vsip_ccfftmop_f 32768x1024 c64 VSIP_ROW, rows N(0,1)*10^U(-3,3)", "f32"
+        rows_check = ("row", M, N, x, y, np.float32, -1, 1.0, N)
+    bx.admit(True)
+    by.admit(False)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda") if nbytes < (512 << 20) else None
+    for _ in range(a.warmup):
+        call()
+    J.check("warm-up")
+    L.jvsip_gpu_synchronize()
+    per = []
+    n0 = L.jvsip_gpu_kernel_launches()
+    for _ in range(a.steps):
+        if flush is not None:
+            with torch.cuda.stream(ext):
+                flush.fill_(1)   # write a buffer larger than L2 between calls (outside the timed events)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        call()
+        e1.record(ext)
+        e1.synchronize()
+        per.append(e0.elapsed_time(e1))
+    launches = L.jvsip_gpu_kernel_launches() - n0
+    J.check("timed loop")
+    ms = statistics.mean(per)
+    by.sync()
+    err = None
+    if rows_check is not None:
+        kind, M_, N_, xx, yy, dty, d, sc, L_ = rows_check
+        errs = []
+        idxs = [0, 1, (M_ if kind == "row" else N_) // 2, (M_ if kind == "row" else N_) - 1]
+        for r in idxs:
+            if kind == "row":
+                xr_ = xx[2 * r * N_: 2 * (r + 1) * N_].astype(np.float64)
+                yr_ = yy[2 * r * N_: 2 * (r + 1) * N_].astype(np.float64)
+            else:
+                xr_ = np.stack([xx[2 * (i * N_ + r): 2 * (i * N_ + r) + 2] for i in range(M_)]).reshape(-1).astype(np.float64)
+                yr_ = np.stack([yy[2 * (i * N_ + r): 2 * (i * N_ + r) + 2] for i in range(M_)]).reshape(-1).astype(np.float64)
+            yo = O.CView(np.zeros(2 * L_), 0, L_, 1, 1, L_)
+            O.Plan(O.CCOP, 1, L_, sc, d, O.ROW, np.float64).ccfftmop(O.CView(xr_, 0, L_, 1, 1, L_), yo)
+            errs.append(float(np.linalg.norm(yr_ - yo.buf) / np.linalg.norm(yo.buf)))
+        err = max(errs)
+    peak, peak_kind = peaks()
+    gbs = nbytes / (ms / 1e3) / 1e9
+    line = {"metric": METRIC, "value": round(gbs, 2), "unit": "GB/s", "n_gpus": 1, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": dt, "data": "synthetic (seeded)",
+            "config": {"workload": desc, "bytes_per_step": nbytes,
+                       "l2": "flushed between calls" if flush is not None else "inputs larger than L2"},
+            "hbm_frac": round(gbs / peak, 4), "rel_l2_vs_fp64_oracle": err, "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(gbs / peak, 4), "peak_kind": peak_kind, "traffic": None}}
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------- GPU arm
 def main():
     global M_ROWS, BYTES_PER_CALL
@@ -180,6 +318,9 @@ def main():
     BYTES_PER_CALL = M_ROWS * N_PTS * 16
     if a.impl == "reference":
         reference_arm(a)
+        return
+    if a.workload != "cfg3":
+        other_workload(a)
         return
     import numpy as np
     import torch

@@ -101,6 +101,7 @@ struct Job {
     const void *tw = nullptr;     // forward table exp(-2 pi i m/N), m < N, dtype complex
     const void *thalf = nullptr;  // R2C/C2R table exp(-+ i pi k/MN), k <= MN
     const void *twp = nullptr;    // per-pass twiddle tables of the specialised kernel (or null)
+    const void *twg = nullptr;    // per-pass twiddle tables of the general kernel's schedule
     int npass = 0;
     int radix[40];
 };
@@ -132,6 +133,7 @@ struct Plan {
     void *d_tw = nullptr;     // forward twiddles, MN entries
     void *d_thalf = nullptr;  // half-angle table, MN+1 entries (real transforms)
     void *d_twp = nullptr;    // per-pass [r][m] twiddle tables of the specialised kernel
+    void *d_twg = nullptr;    // per-pass [r][m] twiddle tables of the general kernel (radix <= 8 schedule)
     std::vector<unsigned long> jofk;  // reference digit-reversal map (kept for parity checks)
     std::mutex mu;            // the plan is used by one call at a time
 };

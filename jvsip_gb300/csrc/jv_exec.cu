@@ -280,6 +280,7 @@ static void fill_job(Job &j, const Plan *p, int kind) {
     j.tw = p->d_tw;
     j.thalf = p->d_thalf;
     j.twp = p->d_twp;
+    j.twg = p->d_twg;
     j.npass = (int)p->radix.size();
     for (int i = 0; i < j.npass && i < 40; i++) j.radix[i] = p->radix[i];
 }

@@ -251,6 +251,7 @@ template <typename T> struct SmemArgs {
     RAcc<T> rin;
     RSto<T> rout;
     const C *tw;      // exp(-2 pi i m/N)
+    const C *twg;     // per-pass tables of the radix schedule, [r][m] each
     const C *thalf;   // exp(-+ i pi k/N), k <= N
 };
 
@@ -259,9 +260,13 @@ template <typename T> struct SmemArgs {
 // (j - m)*R + m + r*Ns, m = j mod Ns, after the twiddle exp(-2 pi i r m/(Ns R)).
 // A thread keeps all its butterflies in registers across the barrier, so the
 // pass needs ceil(EMAX/R) * blockDim >= transforms * N/R.
+__device__ __forceinline__ int spad(int i) { return i + (i >> 4); }
+
 template <typename T, int R, int EMAX>
 __device__ __forceinline__ void smem_pass(typename cplx_t<T>::t *s, int ld, int N, int nt, int Ns,
-                                          const typename cplx_t<T>::t *__restrict__ tw) {
+                                          const typename cplx_t<T>::t *__restrict__ tp) {
+    // tp: this pass's twiddles, entry r*Ns + m = exp(-2 pi i r m/(Ns R)), so the
+    // threads of a warp (consecutive m) read consecutive entries
     typedef typename cplx_t<T>::t C;
     constexpr int K = (EMAX + R - 1) / R;
     const int NR = N / R;
@@ -273,13 +278,12 @@ __device__ __forceinline__ void smem_pass(typename cplx_t<T>::t *s, int ld, int 
         int b = tid + k * nthr;
         if (b < nb) {
             int t = b / NR, j = b - t * NR;
-            const C *src = s + t * ld + j;
+            const C *src = s + t * ld;
 #pragma unroll
-            for (int r = 0; r < R; r++) v[k][r] = src[r * NR];
+            for (int r = 0; r < R; r++) v[k][r] = src[spad(j + r * NR)];
         }
     }
     __syncthreads();
-    const int tstep = N / (Ns * R);
 #pragma unroll
     for (int k = 0; k < K; k++) {
         int b = tid + k * nthr;
@@ -287,14 +291,14 @@ __device__ __forceinline__ void smem_pass(typename cplx_t<T>::t *s, int ld, int 
             int t = b / NR, j = b - t * NR;
             int m = j % Ns;
             if (m) {
-                int st = m * tstep;
 #pragma unroll
-                for (int r = 1; r < R; r++) v[k][r] = cmul(v[k][r], __ldg(&tw[r * st]));
+                for (int r = 1; r < R; r++) v[k][r] = cmul(v[k][r], __ldg(&tp[r * Ns + m]));
             }
             Dft<C, R>::run(v[k]);
-            C *dst = s + t * ld + (j - m) * R + m;
+            C *dst = s + t * ld;
+            const int base = (j - m) * R + m;
 #pragma unroll
-            for (int r = 0; r < R; r++) dst[r * Ns] = v[k][r];
+            for (int r = 0; r < R; r++) dst[spad(base + r * Ns)] = v[k][r];
         }
     }
     __syncthreads();
@@ -303,14 +307,16 @@ __device__ __forceinline__ void smem_pass(typename cplx_t<T>::t *s, int ld, int 
 template <typename T, int EMAX>
 __device__ __forceinline__ void smem_passes(typename cplx_t<T>::t *s, int ld, int N, int nt, int n8, int n4,
                                             int n2, int n3, int n5, int n7,
-                                            const typename cplx_t<T>::t *__restrict__ tw) {
+                                            const typename cplx_t<T>::t *__restrict__ twg) {
+    // passes run in the order of the plan's per-pass tables: 8s, 4, 2, 3s, 5s, 7s
     int Ns = 1;
-    for (int p = 0; p < n8; p++) { smem_pass<T, 8, EMAX>(s, ld, N, nt, Ns, tw); Ns *= 8; }
-    for (int p = 0; p < n4; p++) { smem_pass<T, 4, EMAX>(s, ld, N, nt, Ns, tw); Ns *= 4; }
-    for (int p = 0; p < n2; p++) { smem_pass<T, 2, EMAX>(s, ld, N, nt, Ns, tw); Ns *= 2; }
-    for (int p = 0; p < n3; p++) { smem_pass<T, 3, EMAX>(s, ld, N, nt, Ns, tw); Ns *= 3; }
-    for (int p = 0; p < n5; p++) { smem_pass<T, 5, EMAX>(s, ld, N, nt, Ns, tw); Ns *= 5; }
-    for (int p = 0; p < n7; p++) { smem_pass<T, 7, EMAX>(s, ld, N, nt, Ns, tw); Ns *= 7; }
+    const typename cplx_t<T>::t *tp = twg;
+    for (int p = 0; p < n8; p++) { smem_pass<T, 8, EMAX>(s, ld, N, nt, Ns, tp); tp += 8 * Ns; Ns *= 8; }
+    for (int p = 0; p < n4; p++) { smem_pass<T, 4, EMAX>(s, ld, N, nt, Ns, tp); tp += 4 * Ns; Ns *= 4; }
+    for (int p = 0; p < n2; p++) { smem_pass<T, 2, EMAX>(s, ld, N, nt, Ns, tp); tp += 2 * Ns; Ns *= 2; }
+    for (int p = 0; p < n3; p++) { smem_pass<T, 3, EMAX>(s, ld, N, nt, Ns, tp); tp += 3 * Ns; Ns *= 3; }
+    for (int p = 0; p < n5; p++) { smem_pass<T, 5, EMAX>(s, ld, N, nt, Ns, tp); tp += 5 * Ns; Ns *= 5; }
+    for (int p = 0; p < n7; p++) { smem_pass<T, 7, EMAX>(s, ld, N, nt, Ns, tp); tp += 7 * Ns; Ns *= 7; }
 }
 
 template <typename T, int EMAX, int MAXT>
@@ -342,7 +348,7 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
                 if (a.vec_fast) { t = i % nt; n = i / nt; } else { t = i / N; n = i - t * N; }
                 C c = cin.load(v0 + t, n);
                 if (a.inv) c.y = -c.y;
-                s[t * ld + n] = c;
+                s[t * ld + spad(n)] = c;
             }
         } else if (a.kind == K_R2C) {
             // z_n = x_{2n} + i x_{2n+1}  (c_VSIP_src/VI_rcfftmop_f_def.h:53-75)
@@ -350,7 +356,7 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
             for (int i = tid; i < tot; i += nthr) {
                 int t, n;
                 if (a.vec_fast) { t = i % nt; n = i / nt; } else { t = i / N; n = i - t * N; }
-                s[t * ld + n] = mk<C>(rin.load(v0 + t, 2 * n), rin.load(v0 + t, 2 * n + 1));
+                s[t * ld + spad(n)] = mk<C>(rin.load(v0 + t, 2 * n), rin.load(v0 + t, 2 * n + 1));
             }
         } else {
             // C2R: raw Z_k, k <= N, then the inverse split (VI_crfftmop_f_def.h:58-110)
@@ -358,7 +364,7 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
             for (int i = tid; i < tot; i += nthr) {
                 int t, k;
                 if (a.vec_fast) { t = i % nt; k = i / nt; } else { t = i / (N + 1); k = i - t * (N + 1); }
-                s[t * ld + k] = cin.load(v0 + t, k);
+                s[t * ld + spad(k)] = cin.load(v0 + t, k);
             }
             __syncthreads();
             const int half = N / 2 + 1;   // pairs (k, N-k), k = 0..N/2
@@ -366,7 +372,7 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
             for (int i = tid; i < totp; i += nthr) {
                 int t = i / half, k = i - t * half;
                 C *row = s + t * ld;
-                C f = row[k], b = row[N - k];
+                C f = row[spad(k)], b = row[spad(N - k)];
                 C w = thalf[k];
                 // Y_k = f + b + w.i (b - f) ... with f = Z_k, b = Z_{N-k}, w = exp(+i pi k/N)
                 C yk = mk<C>(f.x + b.x + w.y * (b.x - f.x) - w.x * (f.y + b.y),
@@ -379,20 +385,20 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
                                b.y - f.y - w2.y * (b.y + f.y) + w2.x * (b.x - f.x));
                 }
                 // the inverse transform runs as a forward one on conjugated data
-                row[k] = mk<C>(yk.x, -yk.y);
-                if (pair) row[N - k] = mk<C>(yn.x, -yn.y);
+                row[spad(k)] = mk<C>(yk.x, -yk.y);
+                if (pair) row[spad(N - k)] = mk<C>(yn.x, -yn.y);
             }
         }
         __syncthreads();
         // ---------------- radix passes
-        smem_passes<T, EMAX>(s, ld, N, nt, a.n8, a.n4, a.n2, a.n3, a.n5, a.n7, a.tw);
+        smem_passes<T, EMAX>(s, ld, N, nt, a.n8, a.n4, a.n2, a.n3, a.n5, a.n7, a.twg);
         // ---------------- store phase
         if (a.kind == K_C2C) {
             const int tot = nt * N;
             for (int i = tid; i < tot; i += nthr) {
                 int t, n;
                 if (a.vec_fast) { t = i % nt; n = i / nt; } else { t = i / N; n = i - t * N; }
-                C c = s[t * ld + n];
+                C c = s[t * ld + spad(n)];
                 if (a.inv) c.y = -c.y;
                 if (a.has_scale) c = cscale(c, a.scale);
                 cout.store(v0 + t, n, c);
@@ -404,8 +410,8 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
                 int t, k;
                 if (a.vec_fast) { t = i % nt; k = i / nt; } else { t = i / (N + 1); k = i - t * (N + 1); }
                 const C *row = s + t * ld;
-                C f = row[k == N ? 0 : k];
-                C b = row[k == 0 ? 0 : N - k];
+                C f = row[spad(k == N ? 0 : k)];
+                C b = row[spad(k == 0 ? 0 : N - k)];
                 if (a.has_scale) {
                     f = cscale(f, a.scale);
                     b = cscale(b, a.scale);
@@ -421,7 +427,7 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
             for (int i = tid; i < tot; i += nthr) {
                 int t, n;
                 if (a.vec_fast) { t = i % nt; n = i / nt; } else { t = i / N; n = i - t * N; }
-                C c = s[t * ld + n];
+                C c = s[t * ld + spad(n)];
                 T re = c.x, im = -c.y;
                 if (a.has_scale) {
                     re *= a.scale;

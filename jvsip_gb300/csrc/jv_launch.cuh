@@ -166,7 +166,14 @@ bool launch_smem_t(const Job &j, cudaStream_t st) {
     bool vf_out = labs_(vs_out) == 1 && labs_(es_out) != 1;
     a.vec_fast = (vf_in || vf_out) ? 1 : 0;
     const long N = j.N;
-    long ld = N + (j.kind == K_C2R ? 1 : 0);
+    // shared-memory rows are indexed i + i/16 (conflict-free Stockham passes)
+    const long need = N + (j.kind == K_C2R ? 1 : 0);
+    long ld = (need - 1) + (need - 1) / 16 + 1;
+    a.twg = (const C *)j.twg;
+    if (!a.twg) {
+        set_error(E_ARG, "plan has no per-pass twiddle tables");
+        return false;
+    }
     const long elem_cap = (long)K::EMAX_L * K::MAXT_L;
     long vpb;
     if (a.vec_fast) {

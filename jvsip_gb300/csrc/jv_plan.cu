@@ -128,29 +128,31 @@ static bool make_tables(Plan *p) {
     if (!p->d_tw) return false;
     if (!cuda_ok(cudaMemcpy(p->d_tw, tw.data(), 2 * n * sizeof(T), cudaMemcpyHostToDevice), "twiddle upload"))
         return false;
-    if (sizeof(T) == 4) {
-        // per-pass tables of the specialised kernel: pass with radix R after
-        // radices of product Ns holds exp(-2 pi i r m/(Ns R)) at r*Ns + m
-        std::vector<int> fr = fast_radices(MN);
-        if (!fr.empty()) {
-            std::vector<T> tp;
-            long Ns = 1;
-            for (int R : fr) {
-                for (long r = 0; r < R; r++)
-                    for (long m = 0; m < Ns; m++) {
-                        double c, s;
-                        unit_root((r * m) % (Ns * R), Ns * R, &c, &s);
-                        tp.push_back((T)c);
-                        tp.push_back((T)s);
-                    }
-                Ns *= R;
-            }
-            p->d_twp = dmalloc(tp.size() * sizeof(T));
-            if (!p->d_twp) return false;
-            if (!cuda_ok(cudaMemcpy(p->d_twp, tp.data(), tp.size() * sizeof(T), cudaMemcpyHostToDevice),
-                         "pass twiddle upload"))
-                return false;
+    // per-pass tables: the pass with radix R after radices of product Ns holds
+    // exp(-2 pi i r m/(Ns R)) at r*Ns + m
+    auto pass_tables = [&](const std::vector<int> &radices, void **dst) -> bool {
+        std::vector<T> tp;
+        long Ns = 1;
+        for (int R : radices) {
+            for (long r = 0; r < R; r++)
+                for (long m = 0; m < Ns; m++) {
+                    double c, s;
+                    unit_root((r * m) % (Ns * R), Ns * R, &c, &s);
+                    tp.push_back((T)c);
+                    tp.push_back((T)s);
+                }
+            Ns *= R;
         }
+        if (tp.empty()) tp.assign(2, (T)0);
+        *dst = dmalloc(tp.size() * sizeof(T));
+        if (!*dst) return false;
+        return cuda_ok(cudaMemcpy(*dst, tp.data(), tp.size() * sizeof(T), cudaMemcpyHostToDevice),
+                       "pass twiddle upload");
+    };
+    if (p->smooth && !pass_tables(p->radix, &p->d_twg)) return false;
+    if (sizeof(T) == 4) {
+        std::vector<int> fr = fast_radices(MN);
+        if (!fr.empty() && !pass_tables(fr, &p->d_twp)) return false;
     }
     if (p->type == JV_RCFFTOP || p->type == JV_CRFFTOP) {
         // exp(-i pi k/MN) for R2C, exp(+i pi k/MN) for C2R, k = 0..MN
@@ -178,6 +180,7 @@ static void plan_free(Plan *p) {
     dfree(p->d_tw);
     dfree(p->d_thalf);
     dfree(p->d_twp);
+    dfree(p->d_twg);
     delete p;
 }
 
