@@ -265,6 +265,15 @@ jvsip_fftm_batchplan_f *jvsip_fftm_batch_create_f(size_t n, const vsip_fftm_f *c
 int  jvsip_fftm_batch_run_f(jvsip_fftm_batchplan_f *batch);
 int  jvsip_fftm_batch_destroy_f(jvsip_fftm_batchplan_f *batch);
 
+/* Autotuner of the batching form: for each of the n lengths (2..16384;
+ * vf = 1 for column transforms) time the batch kernel with each candidate
+ * number of FFTs per tile and keep the fastest, in memory and in a versioned
+ * cache file keyed by GPU name ($JVSIP_GPU_TUNE_CACHE, default
+ * ~/.cache/jvsip_gb300/tune-v1.txt).  Untuned lengths use a heuristic.
+ * Returns 0 on success; jvsip_fftm_autotune_entries() counts cached keys. */
+int  jvsip_fftm_autotune_f(size_t n, const unsigned long *lengths, int vf);
+long jvsip_fftm_autotune_entries(void);
+
 /* Library / device information for tools (kernels compiled, SM count). */
 const char *jvsip_gpu_build_info(void);
 /* Device-side synchronisation: returns when all work this library queued has finished. */

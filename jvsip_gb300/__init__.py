@@ -49,7 +49,8 @@ EXPORTS = [
     "jvsip_fftm_setform_f", "jvsip_fftm_getform_f",
     "jvsip_fftm_batch_f", "jvsip_fftm_batch_create_f", "jvsip_fftm_batch_run_f", "jvsip_fftm_batch_destroy_f",
     "jvsip_gpu_build_info", "jvsip_gpu_synchronize", "jvsip_gpu_stream", "jvsip_fftm_passes", "jvsip_fftm_jofk",
-    "jvsip_gpu_kernel_launches", "jvsip_ccfftm_noalloc_f",
+    "jvsip_gpu_kernel_launches", "jvsip_ccfftm_noalloc_f", "jvsip_fftm_autotune_f",
+    "jvsip_fftm_autotune_entries",
 ]
 
 
@@ -140,6 +141,8 @@ def lib(load_only: bool = False):
     L.jvsip_gpu_stream.restype = vp
     L.jvsip_gpu_kernel_launches.restype = C.c_ulong
     L.jvsip_ccfftm_noalloc_f.argtypes = [vp, vp, C.c_long, vp, C.c_long]
+    L.jvsip_fftm_autotune_f.argtypes = [C.c_size_t, vp, C.c_int]
+    L.jvsip_fftm_autotune_entries.restype = C.c_long
     L.jvsip_fftm_setform_f.argtypes = [vp, C.c_int]
     L.jvsip_fftm_getform_f.argtypes = [vp]
     L.jvsip_fftm_batch_f.argtypes = [C.c_size_t, vp, vp, vp]

@@ -1,26 +1,381 @@
-// jv_batch.cu -- batching form: many independent c2c fftm calls in one
-// persistent launch fed by a device work queue.
-#include "jv_core.h"
+// jv_batch.cu -- batching form: many independent c2c fftm calls (uneven
+// lengths 2^a 3^b 5^c 7^d, uneven row counts, mixed directions and ROW/COL
+// majors) in one persistent launch.
+//
+// The host cuts every call into tiles of transforms (FFTs per tile from the
+// autotuner's cache, or the general kernel's heuristic) and uploads one
+// descriptor per tile, largest tiles first.  One launch of 1024-thread CTAs
+// consumes the queue, one descriptor per CTA -- no CTA ever waits on another
+// -- running the general shared-memory passes on each tile.  A captured batch
+// (jvsip_fftm_batch_create_f) records the launch in a CUDA graph once;
+// jvsip_fftm_batch_run_f replays it.
+//
+// No reference counterpart: VSIPL has no multi-plan call; the reference can
+// only loop plan by plan (c_VSIP_src/VI_ccfftmop_f_def.h:20-29 per call).
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <vector>
+
+#include "jv_launch.cuh"
+
+namespace jv {
+
+// one tile: nt transforms [v0, v0+nt) of one call
+struct TileDesc {
+    const float *in;    // interleaved views, complex index off + v*vs + n*es
+    float *out;
+    long in_off, in_es, in_vs;
+    long out_off, out_es, out_vs;
+    const float2 *twg;  // per-pass [r][m] tables of the call's plan
+    long v0;
+    int N, nt, ld;
+    unsigned char n8, n4, n2, n3, n5, n7, inv, vec_fast;
+    int has_scale;
+    float scale;
+};
+
+constexpr int BT = 1024;      // threads of a batch CTA
+constexpr int BEMAX = 16;     // complex values a thread keeps per pass: tiles of <= 16384 points
+
+__device__ __forceinline__ void batch_tile(const TileDesc &d, float2 *s) {
+    const int N = d.N, ld = d.ld, nt = d.nt;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    CAcc<float> cin;
+    cin.re = d.in;
+    cin.im = d.in + 1;
+    cin.cst = 2;
+    cin.off = d.in_off;
+    cin.es = d.in_es;
+    cin.vs = d.in_vs;
+    cin.vec = true;
+    CSto<float> cout;
+    cout.re = d.out;
+    cout.im = d.out + 1;
+    cout.cst = 2;
+    cout.off = d.out_off;
+    cout.es = d.out_es;
+    cout.vs = d.out_vs;
+    cout.vec = true;
+    const int tot = nt * N;
+    for (int i = tid; i < tot; i += nthr) {
+        int t, n;
+        if (d.vec_fast) {
+            t = i % nt;
+            n = i / nt;
+        } else {
+            t = i / N;
+            n = i - t * N;
+        }
+        float2 c = cin.load(d.v0 + t, n);
+        if (d.inv) c.y = -c.y;
+        s[t * ld + spad(n)] = c;
+    }
+    __syncthreads();
+    smem_passes<float, BEMAX>(s, ld, N, nt, d.n8, d.n4, d.n2, d.n3, d.n5, d.n7, d.twg);
+    for (int i = tid; i < tot; i += nthr) {
+        int t, n;
+        if (d.vec_fast) {
+            t = i % nt;
+            n = i / nt;
+        } else {
+            t = i / N;
+            n = i - t * N;
+        }
+        float2 c = s[t * ld + spad(n)];
+        if (d.inv) c.y = -c.y;
+        if (d.has_scale) c = cscale(c, d.scale);
+        cout.store(d.v0 + t, n, c);
+    }
+    __syncthreads();
+}
+
+// One launch over the whole queue: CTA b takes descriptor b.  The queue is
+// sorted largest tile first, so the hardware's in-order CTA dispatch hands the
+// long tiles out first and the short ones fill the tail.  (A persistent
+// variant -- each CTA looping over an atomic queue head -- was built and
+// measured against ptxas: keeping the pass state live across tile iterations
+// spills the codelet registers at every block size, so the loop-free form is
+// used.)
+__global__ void __launch_bounds__(BT, 1) k_batch(const TileDesc *__restrict__ q, int ntiles) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *s = reinterpret_cast<float2 *>(smem_raw);
+    __shared__ TileDesc sd;  // descriptor fields are re-read from shared memory, not held in registers
+    const int t = blockIdx.x;
+    if (t >= ntiles) return;
+    if (threadIdx.x == 0) sd = q[t];
+    __syncthreads();
+    batch_tile(sd, s);
+}
+
+// ---------------------------------------------------------------- host side
+struct BatchBuild {
+    std::vector<TileDesc> tiles;
+    size_t smem = 0;
+    double bytes = 0;
+};
+
+static long tile_ld(long N, bool vf) {
+    long ld = (N - 1) + (N - 1) / 16 + 1;
+    if (vf && (ld % 2 == 0)) ld += 1;
+    return ld;
+}
+
+// FFTs per tile for length N (transforms adjacent in memory or not).
+long batch_fft_per_tile(long N, bool vf, long rows);
+
+static bool build_tiles(size_t n, const vsip_fftm_f *const plans[], const vsip_cmview_f *const in[],
+                        const vsip_cmview_f *const out[], BatchBuild &bb) {
+    Device *d = device();
+    if (!d) return false;
+    for (size_t i = 0; i < n; i++) {
+        Plan *p = plan_of(plans[i]);
+        if (!p || p->prec != P_F32 || (p->type != JV_CCFFTOP && p->type != JV_CCFFTIP)) {
+            set_error(E_ARG, "batch: every plan must be a single-precision c2c plan");
+            return false;
+        }
+        if (!p->smooth || !p->d_twg || p->MN > BEMAX * BT) {
+            set_error(E_UNSUPPORTED, "batch: lengths must be 2^a 3^b 5^c 7^d and at most 16384");
+            return false;
+        }
+        const vsip_cmview_f *x = in[i];
+        const vsip_cmview_f *y = (p->type == JV_CCFFTIP || !out || !out[i]) ? x : out[i];
+        if (!x || !y || !x->block || !y->block) {
+            set_error(E_ARG, "batch: null view");
+            return false;
+        }
+        Mirror *mx = mirror_find(x->block), *my = mirror_find(y->block);
+        if (!mx || !my || x->block->cstride != 2 || y->block->cstride != 2) {
+            set_error(E_ARG, "batch: views must be of admitted interleaved blocks");
+            return false;
+        }
+        const long N = p->MN, nv = p->mN;
+        long xl = (long)(p->major == 0 ? x->row_length : x->col_length);
+        long xn = (long)(p->major == 0 ? x->col_length : x->row_length);
+        long yl = (long)(p->major == 0 ? y->row_length : y->col_length);
+        long yn = (long)(p->major == 0 ? y->col_length : y->row_length);
+        if (xl < N || xn < nv || yl < N || yn < nv) {
+            set_error(E_ARG, "batch: view smaller than its plan");
+            return false;
+        }
+        TileDesc t;
+        memset(&t, 0, sizeof(t));
+        t.in = (const float *)mx->d;
+        t.out = (float *)my->d;
+        t.in_off = (long)x->offset;
+        t.out_off = (long)y->offset;
+        if (p->major == 0) {
+            t.in_es = x->row_stride;
+            t.in_vs = x->col_stride;
+            t.out_es = y->row_stride;
+            t.out_vs = y->col_stride;
+        } else {
+            t.in_es = x->col_stride;
+            t.in_vs = x->row_stride;
+            t.out_es = y->col_stride;
+            t.out_vs = y->row_stride;
+        }
+        // bounds of both views inside their blocks
+        auto span_ok = [&](long off, long es, long vs, long len, long cnt, long size) {
+            long lo = off + std::min(0L, (cnt - 1) * vs) + std::min(0L, (len - 1) * es);
+            long hi = off + std::max(0L, (cnt - 1) * vs) + std::max(0L, (len - 1) * es);
+            return lo >= 0 && hi < size;
+        };
+        if (!span_ok(t.in_off, t.in_es, t.in_vs, N, nv, (long)x->block->size) ||
+            !span_ok(t.out_off, t.out_es, t.out_vs, N, nv, (long)y->block->size)) {
+            set_error(E_ARG, "batch: view outside its block");
+            return false;
+        }
+        if (x->block == y->block && (t.in_off != t.out_off || t.in_es != t.out_es || t.in_vs != t.out_vs)) {
+            set_error(E_UNSUPPORTED, "batch: x and y on one block must be the same view");
+            return false;
+        }
+        t.twg = (const float2 *)p->d_twg;
+        t.N = (int)N;
+        for (int r : p->radix) {
+            switch (r) {
+                case 8: t.n8++; break;
+                case 4: t.n4++; break;
+                case 2: t.n2++; break;
+                case 3: t.n3++; break;
+                case 5: t.n5++; break;
+                case 7: t.n7++; break;
+            }
+        }
+        t.inv = (p->dir == 1) ? 1 : 0;
+        t.has_scale = (p->scale != 1.0) ? 1 : 0;
+        t.scale = (float)p->scale;
+        bool vf_in = labs(t.in_vs) == 1 && labs(t.in_es) != 1;
+        bool vf_out = labs(t.out_vs) == 1 && labs(t.out_es) != 1;
+        t.vec_fast = (vf_in || vf_out) ? 1 : 0;
+        t.ld = (int)tile_ld(N, t.vec_fast);
+        long per = batch_fft_per_tile(N, t.vec_fast, nv);
+        while (per > 1 && per * (long)t.ld * 8 > (long)d->smem_optin) per--;
+        for (long v0 = 0; v0 < nv; v0 += per) {
+            TileDesc u = t;
+            u.v0 = v0;
+            u.nt = (int)std::min(per, nv - v0);
+            bb.tiles.push_back(u);
+            bb.smem = std::max(bb.smem, (size_t)u.nt * u.ld * 8);
+        }
+        bb.bytes += 16.0 * N * nv;
+    }
+    // largest tiles first: the queue's tail is made of short work
+    std::stable_sort(bb.tiles.begin(), bb.tiles.end(), [](const TileDesc &a, const TileDesc &b) {
+        return (long)a.N * a.nt > (long)b.N * b.nt;
+    });
+    return true;
+}
+
+struct DevBatch {
+    TileDesc *q = nullptr;
+    int ntiles = 0;
+    size_t smem = 0;
+};
+
+static bool upload(const BatchBuild &bb, DevBatch &db) {
+    db.ntiles = (int)bb.tiles.size();
+    db.smem = bb.smem;
+    db.q = (TileDesc *)dmalloc(std::max<size_t>(1, bb.tiles.size()) * sizeof(TileDesc));
+    if (!db.q) return false;
+    Device *d = device();
+    if (!bb.tiles.empty() &&
+        !cuda_ok(cudaMemcpyAsync(db.q, bb.tiles.data(), bb.tiles.size() * sizeof(TileDesc),
+                                 cudaMemcpyHostToDevice, d->stream), "batch queue upload"))
+        return false;
+    return true;
+}
+
+static bool launch(const DevBatch &db, cudaStream_t st) {
+    Device *d = device();
+    if (db.ntiles == 0) return true;
+    static bool attr = false;
+    if (!attr) {
+        if (!cuda_ok(cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d->smem_optin),
+                     "cudaFuncSetAttribute"))
+            return false;
+        attr = true;
+    }
+    k_batch<<<db.ntiles, BT, db.smem, st>>>(db.q, db.ntiles);
+    count_launch();
+    return cuda_ok(cudaGetLastError(), "k_batch launch");
+}
+
+static void free_dev(DevBatch &db) {
+    dfree(db.q);
+    db.q = nullptr;
+}
+
+}  // namespace jv
 
 using namespace jv;
 
 struct jvsip_fftm_batchplan_s {
-    int dummy;
+    DevBatch db;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<const void *> blocks;  // output blocks, marked device-newer after a run
 };
 
+static void mark_outputs(size_t n, const vsip_fftm_f *const plans[], const vsip_cmview_f *const in[],
+                         const vsip_cmview_f *const out[]) {
+    for (size_t i = 0; i < n; i++) {
+        Plan *p = plan_of(plans[i]);
+        const vsip_cmview_f *y = (p->type == JV_CCFFTIP || !out || !out[i]) ? in[i] : out[i];
+        Mirror *m = mirror_find(y->block);
+        if (m) m->device_newer = true;
+    }
+}
+
 extern "C" {
+
 int jvsip_fftm_batch_f(size_t n, const vsip_fftm_f *const plans[], const vsip_cmview_f *const in[],
                        const vsip_cmview_f *const out[]) {
-    (void)n; (void)plans; (void)in; (void)out;
-    set_error(E_UNSUPPORTED, "batching form not available");
-    return E_UNSUPPORTED;
+    if (n == 0) return 0;
+    if (!plans || !in) {
+        set_error(E_ARG, "batch: null arrays");
+        return E_ARG;
+    }
+    BatchBuild bb;
+    if (!build_tiles(n, plans, in, out, bb)) return jvsip_gpu_last_error();
+    DevBatch db;
+    Device *d = device();
+    bool ok = upload(bb, db) && launch(db, d->stream);
+    free_dev(db);  // stream-ordered reuse of the pool
+    if (!ok) return jvsip_gpu_last_error() ? jvsip_gpu_last_error() : E_CUDA;
+    mark_outputs(n, plans, in, out);
+    return 0;
 }
+
 jvsip_fftm_batchplan_f *jvsip_fftm_batch_create_f(size_t n, const vsip_fftm_f *const plans[],
                                                   const vsip_cmview_f *const in[], const vsip_cmview_f *const out[]) {
-    (void)n; (void)plans; (void)in; (void)out;
-    set_error(E_UNSUPPORTED, "batching form not available");
-    return nullptr;
+    if (!plans || !in) {
+        set_error(E_ARG, "batch: null arrays");
+        return nullptr;
+    }
+    BatchBuild bb;
+    if (!build_tiles(n, plans, in, out, bb)) return nullptr;
+    jvsip_fftm_batchplan_f *b = new (std::nothrow) jvsip_fftm_batchplan_f();
+    if (!b) {
+        set_error(E_ALLOC, "batch plan");
+        return nullptr;
+    }
+    Device *d = device();
+    if (!upload(bb, b->db) || !cuda_ok(cudaStreamSynchronize(d->stream), "batch upload")) {
+        free_dev(b->db);
+        delete b;
+        return nullptr;
+    }
+    // record the launch once; runs replay the graph
+    cudaStream_t cs = nullptr;
+    bool ok = cuda_ok(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream");
+    ok = ok && cuda_ok(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture");
+    if (ok) {
+        bool lk = launch(b->db, cs);
+        ok = cuda_ok(cudaStreamEndCapture(cs, &b->graph), "end capture") && lk;
+    }
+    ok = ok && cuda_ok(cudaGraphInstantiate(&b->exec, b->graph, 0), "graph instantiate");
+    if (cs) cudaStreamDestroy(cs);
+    if (!ok) {
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        if (b->graph) cudaGraphDestroy(b->graph);
+        free_dev(b->db);
+        delete b;
+        return nullptr;
+    }
+    for (size_t i = 0; i < n; i++) {
+        Plan *p = plan_of(plans[i]);
+        const vsip_cmview_f *y = (p->type == JV_CCFFTIP || !out || !out[i]) ? in[i] : out[i];
+        b->blocks.push_back(y->block);
+    }
+    return b;
 }
-int jvsip_fftm_batch_run_f(jvsip_fftm_batchplan_f *b) { (void)b; return E_UNSUPPORTED; }
-int jvsip_fftm_batch_destroy_f(jvsip_fftm_batchplan_f *b) { (void)b; return 0; }
+
+int jvsip_fftm_batch_run_f(jvsip_fftm_batchplan_f *b) {
+    if (!b) return E_ARG;
+    Device *d = device();
+    if (!d) return E_NODEVICE;
+    if (b->db.ntiles == 0) return 0;
+    if (!cuda_ok(cudaGraphLaunch(b->exec, d->stream), "batch graph launch")) return E_CUDA;
+    count_launch();
+    for (const void *blk : b->blocks) {
+        Mirror *m = mirror_find(blk);
+        if (m) m->device_newer = true;
+    }
+    return 0;
 }
+
+int jvsip_fftm_batch_destroy_f(jvsip_fftm_batchplan_f *b) {
+    if (!b) return 0;
+    Device *d = device();
+    if (d) cudaStreamSynchronize(d->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    free_dev(b->db);
+    delete b;
+    return 0;
+}
+
+}  // extern "C"

@@ -12,7 +12,10 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <map>
+#include <mutex>
 #include <new>
+#include <tuple>
 
 #include "jv_core.h"
 
@@ -111,8 +114,60 @@ static void unit_root(long m, long N, double *c, double *s) {
     *s = flip ? sn : -sn;
 }
 
+// Device tables are shared by all plans of one (length, precision, kind):
+// a batch of thousands of plans over a few hundred lengths keeps one copy.
+struct TableSet {
+    void *tw = nullptr, *thalf = nullptr, *twp = nullptr, *twg = nullptr;
+    int refs = 0;
+};
+static std::mutex g_tab_mu;
+static std::map<std::tuple<long, int, int>, TableSet> g_tabs;
+
+static int table_kind(int type) { return type == JV_RCFFTOP ? 1 : type == JV_CRFFTOP ? 2 : 0; }
+
+template <typename T>
+static bool build_tables(Plan *p);
+
 template <typename T>
 static bool make_tables(Plan *p) {
+    auto key = std::make_tuple(p->MN, p->prec, table_kind(p->type));
+    std::lock_guard<std::mutex> lk(g_tab_mu);
+    auto it = g_tabs.find(key);
+    if (it != g_tabs.end()) {
+        it->second.refs++;
+        p->d_tw = it->second.tw;
+        p->d_thalf = it->second.thalf;
+        p->d_twp = it->second.twp;
+        p->d_twg = it->second.twg;
+        return true;
+    }
+    if (!build_tables<T>(p)) return false;
+    TableSet ts;
+    ts.tw = p->d_tw;
+    ts.thalf = p->d_thalf;
+    ts.twp = p->d_twp;
+    ts.twg = p->d_twg;
+    ts.refs = 1;
+    g_tabs[key] = ts;
+    return true;
+}
+
+static void release_tables(Plan *p) {
+    std::lock_guard<std::mutex> lk(g_tab_mu);
+    auto key = std::make_tuple(p->MN, p->prec, table_kind(p->type));
+    auto it = g_tabs.find(key);
+    if (it != g_tabs.end() && it->second.tw == p->d_tw) {
+        if (--it->second.refs > 0) return;
+        g_tabs.erase(it);
+    }
+    dfree(p->d_tw);
+    dfree(p->d_thalf);
+    dfree(p->d_twp);
+    dfree(p->d_twg);
+}
+
+template <typename T>
+static bool build_tables(Plan *p) {
     long MN = p->MN;
     size_t n = (size_t)(MN > 0 ? MN : 1);
     std::vector<T> tw(2 * n, (T)0);
@@ -177,10 +232,7 @@ static void plan_free(Plan *p) {
     if (!p) return;
     Device *d = device();
     if (d) cudaStreamSynchronize(d->stream);
-    dfree(p->d_tw);
-    dfree(p->d_thalf);
-    dfree(p->d_twp);
-    dfree(p->d_twg);
+    release_tables(p);
     delete p;
 }
 
@@ -231,7 +283,11 @@ static VP *create(int type, vsip_length M, vsip_length N, double scale, int dir,
         for (long i = 0; i < p->MN; i++) p->jofk[i] = ref_jofk((unsigned long)i, pn, p0, pF[ns - 1], ns);
     }
     if (!make_tables<T>(p)) {
-        plan_free(p);
+        dfree(p->d_tw);
+        dfree(p->d_thalf);
+        dfree(p->d_twp);
+        dfree(p->d_twg);
+        delete p;
         free(vp);
         return NULL;
     }
