@@ -212,7 +212,7 @@ static bool build_tiles(size_t n, const vsip_fftm_f *const plans[], const vsip_c
         t.vec_fast = (vf_in || vf_out) ? 1 : 0;
         t.ld = (int)tile_ld(N, t.vec_fast);
         long per = batch_fft_per_tile(N, t.vec_fast, nv);
-        while (per > 1 && per * (long)t.ld * 8 > (long)d->smem_optin) per--;
+        while (per > 1 && per * (long)t.ld * 8 > (long)d->smem_optin - 512) per--;
         for (long v0 = 0; v0 < nv; v0 += per) {
             TileDesc u = t;
             u.v0 = v0;
@@ -253,7 +253,7 @@ static bool launch(const DevBatch &db, cudaStream_t st) {
     if (db.ntiles == 0) return true;
     static bool attr = false;
     if (!attr) {
-        if (!cuda_ok(cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d->smem_optin),
+        if (!cuda_ok(cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d->smem_optin - 512),
                      "cudaFuncSetAttribute"))
             return false;
         attr = true;
