@@ -302,6 +302,11 @@ class FFTM:
         getattr(lib(), "vsip_fftm_getattr" + self.s)(self.h, C.byref(a))
         return a
 
+    def setform(self, form: int):
+        rc = lib().jvsip_fftm_setform_f(self.h, form)
+        if rc:
+            raise RuntimeError("jvsip_fftm_setform_f failed: %d" % rc)
+
     def passes(self):
         buf = (C.c_int * 40)()
         n = lib().jvsip_fftm_passes(self.h, buf, 40)

@@ -233,7 +233,8 @@ void jvsip_gpu_clear_error(void) {
 int jvsip_gpu_synchronize(void) {
     Device *d = device();
     if (!d) return E_NODEVICE;
-    return cuda_ok(cudaStreamSynchronize(d->stream), "cudaStreamSynchronize") ? 0 : E_CUDA;
+    if (!cuda_ok(cudaStreamSynchronize(d->stream), "cudaStreamSynchronize")) return E_CUDA;
+    return split_status_check(d->stream);
 }
 
 int vsip_init(void *ptr) {

@@ -104,6 +104,7 @@ struct Job {
     const void *twg = nullptr;    // per-pass twiddle tables of the general kernel's schedule
     int npass = 0;
     int radix[40];
+    int form = 0;        // JVSIP_FORM_* of the plan
 };
 
 // Kernel entry points (defined in the kernel translation units).
@@ -113,6 +114,8 @@ bool launch_global_f32(const Job &j, cudaStream_t s);
 bool launch_global_f64(const Job &j, cudaStream_t s);
 bool launch_fast_f32(const Job &j, cudaStream_t s);   // specialised kernels; false when none fits
 std::vector<int> fast_radices(long N);                // radix list of the specialised kernel for N
+bool launch_split_f32(const Job &j, cudaStream_t s);  // precision form; false when the call does not qualify
+int split_status_check(cudaStream_t s);               // device status of the precision form (0 = clean)
 
 // Capacity queries used by the dispatcher.
 long smem_max_len(int prec, int kind);   // largest N the shared-memory kernel takes

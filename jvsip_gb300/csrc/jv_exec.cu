@@ -250,6 +250,9 @@ static bool run_job(Job &j, cudaStream_t st) {
             j.radix[i] != 8)
             smooth = false;
     long need = j.N + (j.kind == K_C2R ? 1 : 0);
+    if (j.form == JVSIP_FORM_SPLIT_BF16 || j.form == JVSIP_FORM_SPLIT_FP16) {
+        if (launch_split_f32(j, st)) return jvsip_gpu_last_error() == 0;
+    }
     if (smooth && need <= lim) {
         if (j.prec == P_F32) {
             if (launch_fast_f32(j, st)) return true;
@@ -281,6 +284,7 @@ static void fill_job(Job &j, const Plan *p, int kind) {
     j.thalf = p->d_thalf;
     j.twp = p->d_twp;
     j.twg = p->d_twg;
+    j.form = p->form;
     j.npass = (int)p->radix.size();
     for (int i = 0; i < j.npass && i < 40; i++) j.radix[i] = p->radix[i];
 }

@@ -1,0 +1,72 @@
+"""Precision form: 1024-point rows through the tensor-core DFT products with
+hi/lo-split FP16 (per-row scaled) or BF16 operands and FP32 accumulation,
+against the FP64 oracle on rows whose magnitudes span 10^-3..10^3, forward and
+inverse, in place and out of place; the device status stays clean."""
+import numpy as np
+import pytest
+
+import jvsip_gb300 as J
+import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+M, N = 64, 1024
+
+
+def data(seed):
+    x = O.fill(2 * M * N, seed, 1, np.float32).reshape(M, 2 * N)
+    u = O.fill(M, seed + 1, 0, np.float64) * 3.0
+    return (x * (10.0 ** u).astype(np.float32)[:, None]).reshape(-1)
+
+
+def oracle(x, d, scale):
+    y = O.CView(np.zeros(2 * M * N), 0, N, M, 1, N)
+    O.Plan(O.CCOP, M, N, scale, d, O.ROW, np.float64).ccfftmop(O.CView(x.astype(np.float64), 0, N, M, 1, N), y)
+    return y.buf.reshape(M, 2 * N)
+
+
+def worst_row_err(got, ref):
+    g = got.reshape(M, 2 * N).astype(np.float64)
+    return max(np.linalg.norm(g[r] - ref[r]) / np.linalg.norm(ref[r]) for r in range(M))
+
+
+@pytest.mark.parametrize("form,bound", [(J.JVSIP_FORM_SPLIT_FP16, 1e-6), (J.JVSIP_FORM_SPLIT_BF16, 1e-5)],
+                         ids=["fp16", "bf16"])
+@pytest.mark.parametrize("d", [-1, 1], ids=["fwd", "inv"])
+def test_split_form_accuracy(form, bound, d):
+    L = J.lib()
+    scale = 1.0 if d == -1 else 1.0 / N
+    x = data(21)
+    ref = oracle(x, d, scale)
+    y = np.zeros_like(x)
+    p = J.FFTM(J.KIND_CCOP, M, N, scale, d, J.VSIP_ROW)
+    p.setform(form)
+    assert L.jvsip_fftm_getform_f(p.h) == form
+    bx, by = J.CBlock(x.copy(), admit=True), J.CBlock(y, admit=True, update=False)
+    n0 = L.jvsip_gpu_kernel_launches()
+    p.ccfftmop(bx.view(0, N, M, 1, N), by.view(0, N, M, 1, N))
+    assert L.jvsip_gpu_synchronize() == 0, J.last_error()
+    assert L.jvsip_gpu_kernel_launches() - n0 == 1
+    by.release(True)
+    err = worst_row_err(y, ref)
+    assert err <= bound, f"worst row rel-L2 {err:.3e}"
+
+
+def test_split_form_in_place_and_fallback():
+    L = J.lib()
+    x = data(31)
+    ref = oracle(x, -1, 1.0)
+    p = J.FFTM(J.KIND_CCIP, M, N, 1.0, -1, J.VSIP_ROW)
+    p.setform(J.JVSIP_FORM_SPLIT_FP16)
+    b = J.CBlock(x, admit=True)
+    p.ccfftmip(b.view(0, N, M, 1, N))
+    assert L.jvsip_gpu_synchronize() == 0
+    b.release(True)
+    assert worst_row_err(x, ref) <= 1e-6
+    # shapes the form does not take run on the plain kernels
+    q = J.FFTM(J.KIND_CCOP, 8, 512, 1.0, -1, J.VSIP_ROW)
+    q.setform(J.JVSIP_FORM_SPLIT_BF16)
+    xs = O.fill(2 * 8 * 512, 5, 1, np.float32)
+    ys = np.zeros_like(xs)
+    q.ccfftmop(J.CBlock(xs).view(0, 512, 8, 1, 512), J.CBlock(ys).view(0, 512, 8, 1, 512))
+    assert np.isfinite(ys).all() and np.abs(ys).max() > 0
