@@ -149,19 +149,22 @@ def cpu_leg(x, N, rows_total, gpu_out=None, target_s=10.0, threads=None):
            "sample": f"{rows} of {rows_total} rows x {N} points in {t:.2f} s (oracle/fftm_oracle.c, the reference "
                      "algorithm restated bit for bit; the reference sources are absent on this host)"}
     if gpu_out is not None:
-        G = gpu_out.reshape(-1, 2 * N)
-        sample = sorted({0, 1, rows_total // 3, rows_total - 1})
-        errs_d, errs_f = [], []
+        outs = gpu_out if isinstance(gpu_out, dict) else {"": gpu_out}
+        sample = sorted({0, 1, rows_total // 3, rows_total // 2, rows_total - 1})
+        ref = {}
         for r in sample:
             yo = O.CView(np.zeros(2 * N), 0, N, 1, 1, N)
             O.Plan(O.CCOP, 1, N, 1.0, O.FWD, O.ROW, np.float64).ccfftmop(
                 O.CView(X[r].astype(np.float64), 0, N, 1, 1, N), yo)
-            g = G[r].astype(np.float64)
-            errs_d.append(float(np.linalg.norm(g - yo.buf) / np.linalg.norm(yo.buf)))
-            if r < rows:
-                errs_f.append(float(np.linalg.norm(g - ys[r]) / np.linalg.norm(ys[r])))
-        out["gpu_rel_l2_vs_fp64_oracle"] = max(errs_d)
-        out["gpu_rel_l2_vs_reference_f32"] = max(errs_f) if errs_f else None
+            ref[r] = yo.buf
+        for name, arr in outs.items():
+            G = arr.reshape(-1, 2 * N)
+            errs_d = [float(np.linalg.norm(G[r].astype(np.float64) - ref[r]) / np.linalg.norm(ref[r])) for r in sample]
+            errs_f = [float(np.linalg.norm(G[r].astype(np.float64) - ys[r]) / np.linalg.norm(ys[r]))
+                      for r in sample if r < rows]
+            sfx = ("_" + name) if name else ""
+            out["gpu_rel_l2_vs_fp64_oracle" + sfx] = max(errs_d)
+            out["gpu_rel_l2_vs_reference_f32" + sfx] = max(errs_f) if errs_f else None
     return out
 
 
@@ -309,9 +312,31 @@ def other_workload(a):
     ms = statistics.mean(per)
     extra = {"config": {"workload": desc, "bytes_per_step": nbytes,
                         "l2": "flushed between calls" if flush is not None else "inputs larger than L2"}}
+    outs = {"": y}
+    if w == "cfg4":
+        # the precision forms on the same plan and data: tensor-core DFT products
+        forms = {}
+        for name, form in (("split_fp16", J.JVSIP_FORM_SPLIT_FP16), ("split_bf16", J.JVSIP_FORM_SPLIT_BF16)):
+            plan.setform(form)
+            for _ in range(a.warmup):
+                call()
+            k0 = L.jvsip_gpu_kernel_launches()
+            per_f = timed_calls(torch, ext, call, a.steps, flush)
+            kl = L.jvsip_gpu_kernel_launches() - k0
+            assert L.jvsip_gpu_synchronize() == 0, J.last_error()
+            by.sync()
+            outs[name] = y.copy()
+            msf = statistics.mean(per_f)
+            forms[name] = {"value": round(nbytes / (msf / 1e3) / 1e9, 2), "unit": "GB/s", "ms_per_step": round(msf, 4),
+                           "gpu_launches": int(kl)}
+        plan.setform(J.JVSIP_FORM_PLAIN)
+        extra["forms"] = forms
+        y = outs[""]
     if not a.no_cpu and w in ("cfg1", "cfg4"):
-        extra["cpu_baseline"] = cpu_leg(x, N, M, gpu_out=y, target_s=min(a.cpu_seconds, 3.0))
+        extra["cpu_baseline"] = cpu_leg(x, N, M, gpu_out=outs, target_s=min(a.cpu_seconds, 3.0))
         extra["rel_l2_vs_fp64_oracle"] = extra["cpu_baseline"]["gpu_rel_l2_vs_fp64_oracle"]
+        for name in extra.get("forms", {}):
+            extra["forms"][name]["rel_l2_vs_fp64_oracle"] = extra["cpu_baseline"]["gpu_rel_l2_vs_fp64_oracle_" + name]
     print(json.dumps(line_for(a, nbytes / (ms / 1e3) / 1e9, ms, nbytes, dt, launches, extra)), flush=True)
 
 

@@ -350,10 +350,9 @@ bool launch_split_f32(const Job &j, cudaStream_t st) {
     a.bop = (const uint4 *)g_bop[bf ? 1 : 0];
     a.w1024 = (const float2 *)g_w1024;
     a.status = g_status;
-    // 8 KiB beyond the operands: with the leading and stride byte offsets of
-    // the descriptors read either way round, every operand read stays inside
-    // the CTA's shared memory
-    const size_t smem = SP_A_BYTES + SP_B_BYTES + 8192;
+    // operand reads end at byte 49151 of A and 24575 of B (K step = LBO,
+    // M/N step = SBO): inside the two operands
+    const size_t smem = SP_A_BYTES + SP_B_BYTES;
     static bool attr[2] = {false, false};
     if (!attr[bf]) {
         cudaError_t e = bf ? cudaFuncSetAttribute(k_split1024<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
