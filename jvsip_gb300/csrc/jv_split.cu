@@ -3,19 +3,24 @@
 //
 // A row x (n = 32a + b) is a 32 x 32 matrix X[a][b].  Its DFT is the
 // four-step  Z = F32^T-applied over a,  Z'[c][b] = Z[c][b] * w1024^(bc),
-// X[c + 32d] = sum_b Z'[c][b] w32^(bd).  Each step is a real GEMM of a
-// 128 x 192 A operand (4 rows x 32 vectors, K = {hi, lo, hi} x {re, im} x 32)
-// with a 64 x 192 B operand (the 32-point DFT matrix, {hi, hi, lo} x the 2x2
-// real form of complex multiplication), so the three products
-// hi*hi + lo*hi + hi*lo recover about 22 (FP16) or 16 (BF16) significant
-// bits of each operand while the tensor core accumulates in FP32.  FP16
-// operands are scaled per row by a power of two before the split (so their
-// range fits FP16); BF16 operands are not scaled.  The inverse direction runs
-// as conj(F(conj x)); the user scale is applied at the store.
+// X[c + 32d] = sum_b Z'[c][b] w32^(bd).  Each step is a real GEMM whose A
+// operand is 128 x 128 (4 rows x 32 vectors; K = {hi, lo} x {re, im} x 32)
+// and whose B operand is 64 x 128 (the 32-point DFT matrix in the 2x2 real
+// form of complex multiplication, K = {W_hi, W_lo} x {re, im} x 32).  Three
+// products accumulate into one FP32 tensor-memory tile:
+//     X_hi * W_hi  +  X_lo * W_hi  +  X_hi * W_lo
+// (A K-blocks 0-3 with B 0-3, A 4-7 with B 0-3, A 0-3 with B 4-7), which
+// recovers about 22 (FP16) or 16 (BF16) significant bits of each operand.
+// FP16 operands are scaled per row by a power of two before the split (so
+// their range fits FP16); BF16 operands are not scaled.  The inverse
+// direction runs as conj(F(conj x)); the user scale is applied at the store.
 //
-// Per CTA: 128 threads, one warp per row; TMEM holds the two 128 x 64 FP32
-// accumulators (128 columns); one elected thread issues 12 tcgen05.mma per
-// step and commits them to an mbarrier the CTA waits on with a bounded loop.
+// Per CTA: 128 threads, one warp per row; 64 tensor-memory columns hold the
+// 128 x 64 FP32 accumulator of step 1 and then of step 2; one elected thread
+// issues 12 tcgen05.mma per step and commits them to an mbarrier the CTA
+// waits on with a bounded loop.  The A operand's K-blocks are 2064 bytes
+// apart (2048 + 16) so that the step-2 stores, which run along K, spread
+// over all shared-memory banks.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <stdint.h>
@@ -32,18 +37,21 @@
 
 namespace jv {
 
-constexpr int SPN = 1024;            // transform length of the form
-constexpr int SPM = 128;             // GEMM M: 4 rows x 32
-constexpr int SPK = 192;             // GEMM K
-constexpr int SPNN = 64;             // GEMM N
-constexpr int SP_A_BYTES = SPM * SPK * 2;
-constexpr int SP_B_BYTES = SPNN * SPK * 2;
+constexpr int SPN = 1024;                        // transform length of the form
+constexpr int SPM = 128;                         // GEMM M: 4 rows x 32
+constexpr int SPK = 128;                         // operand K: {hi, lo} x {re, im} x 32
+constexpr int SPNN = 64;                         // GEMM N: {re, im} x 32
+constexpr uint32_t SP_A_LBO = (SPM / 8) * 128 + 16;  // bytes between K-adjacent core matrices of A
+constexpr uint32_t SP_B_LBO = (SPNN / 8) * 128;      // the same for B (unpadded)
+constexpr int SP_A_BYTES = (SPK / 8) * SP_A_LBO;     // 33024
+constexpr int SP_B_BYTES = (SPK / 8) * SP_B_LBO;     // 16384
+constexpr int SP_TMEM_COLS = 64;
 constexpr uint32_t SP_WAIT_LIMIT = 1u << 24;
 
-// byte offset of element (row, k) of a K-major operand with `rows` rows laid out as
-// no-swizzle core matrices: [k/8][row/8][row%8][k%8]
-__host__ __device__ __forceinline__ uint32_t core_off(int row, int k, int rows) {
-    return (uint32_t)((((k >> 3) * (rows >> 3) + (row >> 3)) << 7) + ((row & 7) << 4) + ((k & 7) << 1));
+// byte offset of element (row, k) of a K-major no-swizzle operand made of
+// 8-row x 16-byte core matrices: [k/8] (lbo apart) [row/8] (128 apart) [row%8][k%8]
+__host__ __device__ __forceinline__ uint32_t core_off(int row, int k, uint32_t lbo) {
+    return (uint32_t)(k >> 3) * lbo + (uint32_t)((row >> 3) << 7) + (uint32_t)((row & 7) << 4) + (uint32_t)((k & 7) << 1);
 }
 
 struct SplitArgs {
@@ -54,19 +62,41 @@ struct SplitArgs {
     int inv, has_scale;
     float scale;
     const uint4 *bop;     // B operand, SP_B_BYTES in core-matrix layout
-    const float2 *w1024;  // exp(-2 pi i m/1024)
+    const float2 *tw;     // [c][b] = exp(-2 pi i bc/1024), c, b < 32
     int *status;          // set to 1 when a barrier wait expired
 };
 
+// two floats -> one 32-bit word of two 16-bit values (first in the low half),
+// and back
 template <bool BF>
-__device__ __forceinline__ uint16_t to16(float x) {
-    if (BF) return __bfloat16_as_ushort(__float2bfloat16_rn(x));
-    return __half_as_ushort(__float2half_rn(x));
+__device__ __forceinline__ uint32_t pack2(float lo, float hi) {
+    uint32_t u;
+    if (BF) {
+        __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+        memcpy(&u, &h, 4);
+    } else {
+        __half2 h = __floats2half2_rn(lo, hi);
+        memcpy(&u, &h, 4);
+    }
+    return u;
 }
 template <bool BF>
-__device__ __forceinline__ float from16(uint16_t h) {
-    if (BF) return __bfloat162float(__ushort_as_bfloat16(h));
-    return __half2float(__ushort_as_half(h));
+__device__ __forceinline__ float2 unpack2(uint32_t u) {
+    if (BF) {
+        __nv_bfloat162 h;
+        memcpy(&h, &u, 4);
+        return __bfloat1622float2(h);
+    }
+    __half2 h;
+    memcpy(&h, &u, 4);
+    return __half22float2(h);
+}
+// hi word and lo word of the split of (x0, x1)
+template <bool BF>
+__device__ __forceinline__ void split2(float x0, float x1, uint32_t &hi, uint32_t &lo) {
+    hi = pack2<BF>(x0, x1);
+    const float2 f = unpack2<BF>(hi);
+    lo = pack2<BF>(x0 - f.x, x1 - f.y);
 }
 
 // power-of-two scale bringing the warp's largest magnitude into [2^13, 2^14)
@@ -78,11 +108,33 @@ __device__ __forceinline__ float warp_scale(float m) {
     return ldexpf(1.f, 13 - e);
 }
 
+// the three products of one step into tensor memory at `d`
+__device__ __forceinline__ void split_mma(uint32_t d, uint32_t a0, uint32_t b0, uint32_t idesc) {
+#pragma unroll 1
+    for (int i = 0; i < 12; i++) {
+        const int ka = (i < 8) ? i : i - 8;  // A K-chunk: hi 0-3, lo 4-7, hi 0-3
+        const int kb = (i < 4) ? i : i - 4;  // B K-chunk: W_hi 0-3, W_hi 0-3, W_lo 4-7
+        tc::mma_f16(d, tc::smem_desc(a0 + ka * 2 * SP_A_LBO, SP_A_LBO, 128),
+                    tc::smem_desc(b0 + kb * 2 * SP_B_LBO, SP_B_LBO, 128), idesc, i > 0);
+    }
+}
+
+// 32 accumulator columns of this warp's lanes, from column `col`
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    float t[16];
+    tc::tmem_ld16(taddr, t);
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = t[i];
+    tc::tmem_ld16(taddr + 16, t);
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[16 + i] = t[i];
+}
+
 template <bool BF>
-__global__ void __launch_bounds__(128) k_split1024(const SplitArgs a) {
+__global__ void __launch_bounds__(128, 4) k_split1024(const SplitArgs a) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *Asm = smem;                     // 48 KiB, 1024-aligned
-    unsigned char *Bsm = smem + SP_A_BYTES;        // 24 KiB
+    unsigned char *Bsm = smem;                     // 16 KiB
+    unsigned char *Asm = smem + SP_B_BYTES;        // 33024 bytes
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tslot;
     const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
@@ -90,14 +142,15 @@ __global__ void __launch_bounds__(128) k_split1024(const SplitArgs a) {
     const bool live = row < a.nvec;
 
     if (w == 0) {
-        tc::tmem_alloc(&tslot, 128);
+        tc::tmem_alloc(&tslot, SP_TMEM_COLS);
         tc::tmem_relinquish();
     }
     if (tid == 0) tc::mbar_init(&mbar, 1);
     // B operand (constant per plan) into shared memory
     {
         uint4 *dst = reinterpret_cast<uint4 *>(Bsm);
-        for (int i = tid; i < SP_B_BYTES / 16; i += 128) dst[i] = __ldg(&a.bop[i]);
+#pragma unroll
+        for (int i = 0; i < SP_B_BYTES / 16 / 128; i++) dst[tid + 128 * i] = __ldg(&a.bop[tid + 128 * i]);
     }
     // ---- step 1 operand: thread (w, l) owns vector b = l of row w: x[32a + l], a < 32
     float2 v[32];
@@ -112,34 +165,22 @@ __global__ void __launch_bounds__(128) k_split1024(const SplitArgs a) {
     }
     const float s1 = BF ? 1.f : warp_scale(mx);
     {
-        const int m = w * 32 + l;
-        // k = part*64 + ri*32 + a; parts: X_hi, X_lo, X_hi
+        // k = part*64 + ri*32 + a: K-block ab (re hi), 4+ab (im hi), 8+ab (re lo), 12+ab (im lo)
+        unsigned char *arow = Asm + core_off(w * 32 + l, 0, SP_A_LBO);
 #pragma unroll
         for (int ab = 0; ab < 4; ab++) {
-            uint16_t hr[8], hi_[8], lr[8], li[8];
+            uint4 hr, hi, lr, li;
+            uint32_t *phr = &hr.x, *phi = &hi.x, *plr = &lr.x, *pli = &li.x;
 #pragma unroll
-            for (int q = 0; q < 8; q++) {
-                float xr = v[ab * 8 + q].x * s1, xi = v[ab * 8 + q].y * s1;
-                hr[q] = to16<BF>(xr);
-                hi_[q] = to16<BF>(xi);
-                lr[q] = to16<BF>(xr - from16<BF>(hr[q]));
-                li[q] = to16<BF>(xi - from16<BF>(hi_[q]));
+            for (int q = 0; q < 4; q++) {
+                const float2 e0 = v[ab * 8 + 2 * q], e1 = v[ab * 8 + 2 * q + 1];
+                split2<BF>(e0.x * s1, e1.x * s1, phr[q], plr[q]);
+                split2<BF>(e0.y * s1, e1.y * s1, phi[q], pli[q]);
             }
-            uint4 phr, phi, plr, pli;
-            phr.x = hr[0] | (uint32_t)hr[1] << 16; phr.y = hr[2] | (uint32_t)hr[3] << 16;
-            phr.z = hr[4] | (uint32_t)hr[5] << 16; phr.w = hr[6] | (uint32_t)hr[7] << 16;
-            phi.x = hi_[0] | (uint32_t)hi_[1] << 16; phi.y = hi_[2] | (uint32_t)hi_[3] << 16;
-            phi.z = hi_[4] | (uint32_t)hi_[5] << 16; phi.w = hi_[6] | (uint32_t)hi_[7] << 16;
-            plr.x = lr[0] | (uint32_t)lr[1] << 16; plr.y = lr[2] | (uint32_t)lr[3] << 16;
-            plr.z = lr[4] | (uint32_t)lr[5] << 16; plr.w = lr[6] | (uint32_t)lr[7] << 16;
-            pli.x = li[0] | (uint32_t)li[1] << 16; pli.y = li[2] | (uint32_t)li[3] << 16;
-            pli.z = li[4] | (uint32_t)li[5] << 16; pli.w = li[6] | (uint32_t)li[7] << 16;
-            *reinterpret_cast<uint4 *>(Asm + core_off(m, 0 + ab * 8, SPM)) = phr;
-            *reinterpret_cast<uint4 *>(Asm + core_off(m, 32 + ab * 8, SPM)) = phi;
-            *reinterpret_cast<uint4 *>(Asm + core_off(m, 64 + ab * 8, SPM)) = plr;
-            *reinterpret_cast<uint4 *>(Asm + core_off(m, 96 + ab * 8, SPM)) = pli;
-            *reinterpret_cast<uint4 *>(Asm + core_off(m, 128 + ab * 8, SPM)) = phr;
-            *reinterpret_cast<uint4 *>(Asm + core_off(m, 160 + ab * 8, SPM)) = phi;
+            *reinterpret_cast<uint4 *>(arow + (0 + ab) * SP_A_LBO) = hr;
+            *reinterpret_cast<uint4 *>(arow + (4 + ab) * SP_A_LBO) = hi;
+            *reinterpret_cast<uint4 *>(arow + (8 + ab) * SP_A_LBO) = lr;
+            *reinterpret_cast<uint4 *>(arow + (12 + ab) * SP_A_LBO) = li;
         }
     }
     tc::fence_async_smem();
@@ -149,12 +190,8 @@ __global__ void __launch_bounds__(128) k_split1024(const SplitArgs a) {
     const uint32_t tbase = tslot;
     const uint32_t idesc = tc::idesc_f16(SPM, SPNN, BF ? 1 : 0);
     const uint32_t a0 = tc::smem_addr(Asm), b0 = tc::smem_addr(Bsm);
-    const uint32_t lbo_a = (SPM / 8) * 128, lbo_b = (SPNN / 8) * 128, sbo = 128;
     if (tid == 0) {
-#pragma unroll 1
-        for (int kc = 0; kc < SPK / 16; kc++)
-            tc::mma_f16(tbase, tc::smem_desc(a0 + kc * 2 * lbo_a, lbo_a, sbo), tc::smem_desc(b0 + kc * 2 * lbo_b, lbo_b, sbo),
-                        idesc, kc > 0);
+        split_mma(tbase, a0, b0, idesc);
         tc::mma_commit(&mbar);
     }
     bool ok = tc::mbar_wait(&mbar, 0, SP_WAIT_LIMIT);
@@ -165,55 +202,50 @@ __global__ void __launch_bounds__(128) k_split1024(const SplitArgs a) {
     float zr[32], zi[32];
     const uint32_t lane_base = tbase + ((uint32_t)(w * 32) << 16);
     if (ok) {
-        float t[16];
-        tc::tmem_ld16(lane_base + 0, t);
-#pragma unroll
-        for (int i = 0; i < 16; i++) zr[i] = t[i];
-        tc::tmem_ld16(lane_base + 16, t);
-#pragma unroll
-        for (int i = 0; i < 16; i++) zr[16 + i] = t[i];
-        tc::tmem_ld16(lane_base + 32, t);
-#pragma unroll
-        for (int i = 0; i < 16; i++) zi[i] = t[i];
-        tc::tmem_ld16(lane_base + 48, t);
-#pragma unroll
-        for (int i = 0; i < 16; i++) zi[16 + i] = t[i];
+        tmem_ld32(lane_base + 0, zr);
+        tmem_ld32(lane_base + 32, zi);
         tc::tmem_ld_wait();
     }
-    // twiddle w1024^(b c), b = l
+    // twiddle w1024^(b c), b = l: table row c is contiguous over b
     mx = 0.f;
 #pragma unroll
     for (int c = 0; c < 32; c++) {
-        float2 tw = __ldg(&a.w1024[(l * c) & (SPN - 1)]);
-        float r = zr[c] * tw.x - zi[c] * tw.y, i = zr[c] * tw.y + zi[c] * tw.x;
+        const float2 t = __ldg(&a.tw[c * 32 + l]);
+        const float r = zr[c] * t.x - zi[c] * t.y, i = zr[c] * t.y + zi[c] * t.x;
         zr[c] = r;
         zi[c] = i;
         mx = fmaxf(mx, fmaxf(fabsf(r), fabsf(i)));
     }
     const float s2 = BF ? 1.f : warp_scale(mx);
-    // ---- step 2 operand: A2[(w, c)][part*64 + ri*32 + b], b = l (overwrites A after step 1)
+    // ---- step 2 operand: A2[(w, c)][part*64 + ri*32 + b], b = l, written over
+    // step 1's operand.  Lane pairs (l, l^1) trade one word so that each lane
+    // stores two 4-byte pairs of adjacent b: even lanes (re hi, im hi) at b = l,
+    // odd lanes (re lo, im lo) at b = l - 1.  The two stores are ordered so the
+    // even and odd halves of the warp fall in different banks.
+    {
+        const bool even = (l & 1) == 0;
+        const int k1 = even ? l : 96 + l - 1, k2 = even ? 32 + l : 64 + l - 1;
+        unsigned char *p1 = Asm + core_off(w * 32, k1, SP_A_LBO);
+        unsigned char *p2 = Asm + core_off(w * 32, k2, SP_A_LBO);
 #pragma unroll
-    for (int c = 0; c < 32; c++) {
-        const int m = w * 32 + c;
-        float xr = zr[c] * s2, xi = zi[c] * s2;
-        uint16_t hr = to16<BF>(xr), hi_ = to16<BF>(xi);
-        uint16_t lr = to16<BF>(xr - from16<BF>(hr)), li = to16<BF>(xi - from16<BF>(hi_));
-        *reinterpret_cast<uint16_t *>(Asm + core_off(m, l, SPM)) = hr;
-        *reinterpret_cast<uint16_t *>(Asm + core_off(m, 32 + l, SPM)) = hi_;
-        *reinterpret_cast<uint16_t *>(Asm + core_off(m, 64 + l, SPM)) = lr;
-        *reinterpret_cast<uint16_t *>(Asm + core_off(m, 96 + l, SPM)) = li;
-        *reinterpret_cast<uint16_t *>(Asm + core_off(m, 128 + l, SPM)) = hr;
-        *reinterpret_cast<uint16_t *>(Asm + core_off(m, 160 + l, SPM)) = hi_;
+        for (int c = 0; c < 32; c++) {
+            uint32_t P, Q;  // (re hi | im hi << 16), (re lo | im lo << 16)
+            split2<BF>(zr[c] * s2, zi[c] * s2, P, Q);
+            const uint32_t R = __shfl_xor_sync(0xffffffffu, even ? Q : P, 1);
+            const uint32_t X = even ? P : R, Y = even ? R : Q;
+            const uint32_t wlo = __byte_perm(X, Y, 0x5410), whi = __byte_perm(X, Y, 0x7632);
+            const uint32_t mo = (uint32_t)((c >> 3) << 7) + (uint32_t)((c & 7) << 4);
+            *reinterpret_cast<uint32_t *>(p1 + mo) = even ? wlo : whi;
+            *reinterpret_cast<uint32_t *>(p2 + mo) = even ? whi : wlo;
+        }
     }
+    // the step 1 accumulator is read out: step 2 reuses its columns
     tc::fence_async_smem();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     if (tid == 0 && ok) {
-#pragma unroll 1
-        for (int kc = 0; kc < SPK / 16; kc++)
-            tc::mma_f16(tbase + SPNN, tc::smem_desc(a0 + kc * 2 * lbo_a, lbo_a, sbo),
-                        tc::smem_desc(b0 + kc * 2 * lbo_b, lbo_b, sbo), idesc, kc > 0);
+        split_mma(tbase, a0, b0, idesc);
         tc::mma_commit(&mbar);
     }
     if (ok) {
@@ -224,19 +256,9 @@ __global__ void __launch_bounds__(128) k_split1024(const SplitArgs a) {
     tc::fence_after_sync();
     // ---- step 2 result: lane (w, l) = (row, c = l), columns re d | im d -> out[c + 32 d]
     if (ok) {
-        float yr[32], yi[32], t[16];
-        tc::tmem_ld16(lane_base + SPNN + 0, t);
-#pragma unroll
-        for (int i = 0; i < 16; i++) yr[i] = t[i];
-        tc::tmem_ld16(lane_base + SPNN + 16, t);
-#pragma unroll
-        for (int i = 0; i < 16; i++) yr[16 + i] = t[i];
-        tc::tmem_ld16(lane_base + SPNN + 32, t);
-#pragma unroll
-        for (int i = 0; i < 16; i++) yi[i] = t[i];
-        tc::tmem_ld16(lane_base + SPNN + 48, t);
-#pragma unroll
-        for (int i = 0; i < 16; i++) yi[16 + i] = t[i];
+        float yr[32], yi[32];
+        tmem_ld32(lane_base + 0, yr);
+        tmem_ld32(lane_base + 32, yi);
         tc::tmem_ld_wait();
         if (live) {
             const float f = (a.has_scale ? a.scale : 1.f) / (s1 * s2);
@@ -255,14 +277,15 @@ __global__ void __launch_bounds__(128) k_split1024(const SplitArgs a) {
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (w == 0) tc::tmem_dealloc(tbase, 128);
+    if (w == 0) tc::tmem_dealloc(tbase, SP_TMEM_COLS);
 }
 
 // ---------------------------------------------------------------- host side
 // B operand of both steps: row n = ro*32 + c, column k = part*64 + ri*32 + a,
 // the real 2x2 form of w32^(ac) = exp(-2 pi i ac/32) (FP64, then split):
-// (ro, ri) = (re, re): cos, (re, im): +sin, (im, re): -sin, (im, im): cos;
-// parts {hi, hi, lo} pair with the A parts {hi, lo, hi}.
+// (ro, ri) = (re, re): cos, (re, im): -sin, (im, re): +sin, (im, im): cos;
+// part 0 holds the 16-bit rounding W_hi of each entry, part 1 the rounding
+// W_lo of its remainder.
 template <bool BF>
 static std::vector<uint16_t> b_operand() {
     std::vector<uint16_t> b(SP_B_BYTES / 2, 0);
@@ -287,37 +310,35 @@ static std::vector<uint16_t> b_operand() {
                         lo = __half_as_ushort(__float2half_rn((float)(val - (double)__half2float(h))));
                     }
                     const int n = ro * 32 + c;
-                    const uint16_t parts[3] = {hi, hi, lo};
-                    for (int part = 0; part < 3; part++) {
-                        int k = part * 64 + ri * 32 + aa;
-                        b[core_off(n, k, SPNN) / 2] = parts[part];
-                    }
+                    b[core_off(n, 0 * 64 + ri * 32 + aa, SP_B_LBO) / 2] = hi;
+                    b[core_off(n, 1 * 64 + ri * 32 + aa, SP_B_LBO) / 2] = lo;
                 }
     return b;
 }
 
 static std::mutex g_sp_mu;
 static void *g_bop[2] = {nullptr, nullptr};
-static void *g_w1024 = nullptr;
+static void *g_tw = nullptr;
 static int *g_status = nullptr;
 
 static bool split_tables() {
-    if (g_bop[0] && g_bop[1] && g_w1024 && g_status) return true;
+    if (g_bop[0] && g_bop[1] && g_tw && g_status) return true;
     std::vector<uint16_t> b16 = b_operand<false>(), bbf = b_operand<true>();
-    std::vector<float> w(2 * SPN);
-    for (int m = 0; m < SPN; m++) {
-        double ang = -2.0 * 3.14159265358979323846264338327950288 * (double)m / SPN;
-        w[2 * m] = (float)cos(ang);
-        w[2 * m + 1] = (float)sin(ang);
-    }
+    std::vector<float> w(2 * 32 * 32);
+    for (int c = 0; c < 32; c++)
+        for (int bb = 0; bb < 32; bb++) {
+            double ang = -2.0 * 3.14159265358979323846264338327950288 * (double)(bb * c) / SPN;
+            w[2 * (c * 32 + bb)] = (float)cos(ang);
+            w[2 * (c * 32 + bb) + 1] = (float)sin(ang);
+        }
     g_bop[0] = dmalloc(SP_B_BYTES);
     g_bop[1] = dmalloc(SP_B_BYTES);
-    g_w1024 = dmalloc(w.size() * sizeof(float));
+    g_tw = dmalloc(w.size() * sizeof(float));
     g_status = (int *)dmalloc(sizeof(int));
-    if (!g_bop[0] || !g_bop[1] || !g_w1024 || !g_status) return false;
+    if (!g_bop[0] || !g_bop[1] || !g_tw || !g_status) return false;
     return cuda_ok(cudaMemcpy(g_bop[0], b16.data(), SP_B_BYTES, cudaMemcpyHostToDevice), "split tables") &&
            cuda_ok(cudaMemcpy(g_bop[1], bbf.data(), SP_B_BYTES, cudaMemcpyHostToDevice), "split tables") &&
-           cuda_ok(cudaMemcpy(g_w1024, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice), "split tables") &&
+           cuda_ok(cudaMemcpy(g_tw, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice), "split tables") &&
            cuda_ok(cudaMemset(g_status, 0, sizeof(int)), "split status");
 }
 
@@ -348,10 +369,11 @@ bool launch_split_f32(const Job &j, cudaStream_t st) {
     a.has_scale = j.has_scale;
     a.scale = (float)j.scale;
     a.bop = (const uint4 *)g_bop[bf ? 1 : 0];
-    a.w1024 = (const float2 *)g_w1024;
+    a.tw = (const float2 *)g_tw;
     a.status = g_status;
-    // operand reads end at byte 49151 of A and 24575 of B (K step = LBO,
-    // M/N step = SBO): inside the two operands
+    // operand reads: A chunks start at 2 * ka * SP_A_LBO (ka < 8) and span two
+    // K-blocks of 16 x 128 bytes, ending at byte 16 * SP_A_LBO - 17 of A; B
+    // chunks end at byte 16 * SP_B_LBO - 1 of B: both inside their operands
     const size_t smem = SP_A_BYTES + SP_B_BYTES;
     static bool attr[2] = {false, false};
     if (!attr[bf]) {
