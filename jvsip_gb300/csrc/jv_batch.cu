@@ -60,34 +60,24 @@ __device__ __forceinline__ void batch_tile(const TileDesc &d, float2 *s) {
     cout.vs = d.out_vs;
     cout.vec = true;
     const int tot = nt * N;
-    for (int i = tid; i < tot; i += nthr) {
-        int t, n;
-        if (d.vec_fast) {
-            t = i % nt;
-            n = i / nt;
-        } else {
-            t = i / N;
-            n = i - t * N;
-        }
-        float2 c = cin.load(d.v0 + t, n);
+    const bool vf = d.vec_fast != 0;
+    Walk w;
+    walk_tile(w, vf, nt, N, cin.vs, cin.es, cin.off + d.v0 * cin.vs);
+    for (int i = tid; i < tot; i += nthr, w.next()) {
+        const int t = vf ? w.b : w.a, n = vf ? w.a : w.b;
+        float2 c = cin.at(w.g);
         if (d.inv) c.y = -c.y;
         s[t * ld + spad(n)] = c;
     }
     __syncthreads();
     smem_passes<float, BEMAX>(s, ld, N, nt, d.n8, d.n4, d.n2, d.n3, d.n5, d.n7, d.twg);
-    for (int i = tid; i < tot; i += nthr) {
-        int t, n;
-        if (d.vec_fast) {
-            t = i % nt;
-            n = i / nt;
-        } else {
-            t = i / N;
-            n = i - t * N;
-        }
+    walk_tile(w, vf, nt, N, cout.vs, cout.es, cout.off + d.v0 * cout.vs);
+    for (int i = tid; i < tot; i += nthr, w.next()) {
+        const int t = vf ? w.b : w.a, n = vf ? w.a : w.b;
         float2 c = s[t * ld + spad(n)];
         if (d.inv) c.y = -c.y;
         if (d.has_scale) c = cscale(c, d.scale);
-        cout.store(d.v0 + t, n, c);
+        cout.put(w.g, c);
     }
     __syncthreads();
 }

@@ -202,6 +202,11 @@ template <typename T> struct CAcc {
         if (vec) return *reinterpret_cast<const C *>(re + i);
         return mk<C>(re[i], im[i]);
     }
+    // element at complex index g (= off + v*vs + n*es)
+    __device__ __forceinline__ C at(long g) const {
+        if (vec) return reinterpret_cast<const C *>(re)[g];
+        return mk<C>(re[cst * g], im[cst * g]);
+    }
 };
 template <typename T> struct CSto {
     typedef typename cplx_t<T>::t C;
@@ -218,6 +223,14 @@ template <typename T> struct CSto {
             im[i] = c.y;
         }
     }
+    __device__ __forceinline__ void put(long g, C c) const {
+        if (vec) {
+            reinterpret_cast<C *>(re)[g] = c;
+        } else {
+            re[cst * g] = c.x;
+            im[cst * g] = c.y;
+        }
+    }
 };
 template <typename T> struct RAcc {
     const T *a;
@@ -228,6 +241,39 @@ template <typename T> struct RSto {
     T *a;
     long rst, off, es, vs;
     __device__ __forceinline__ void store(long v, long n, T x) const { a[rst * (off + v * vs + n * es)] = x; }
+};
+
+// floor(x / d) by a multiply-high with m = ceil(2^32 / d), exact whenever
+// x * d < 2^32 (every index of one CTA's tile: x, d < 2^16); m = 0 encodes d = 1
+__device__ __forceinline__ unsigned magic_of(unsigned d) { return d <= 1 ? 0u : 0xFFFFFFFFu / d + 1u; }
+__device__ __forceinline__ int mdiv(int x, unsigned m) { return m ? (int)__umulhi((unsigned)x, m) : x; }
+
+// Walks i = i0, i0 + step, ... over an A x B grid (i = a*B + b, b fastest)
+// keeping the global element index g = g0 + a*sa + b*sb up to date with adds:
+// one division per thread at the start, none per element.
+struct Walk {
+    int a, b, B, da, db;
+    long g, dg, dgw;
+    __device__ __forceinline__ void init(int i0, int step, int B_, long sa, long sb, long g0) {
+        B = B_;
+        a = i0 / B;
+        b = i0 - a * B;
+        da = step / B;
+        db = step - da * B;
+        g = g0 + (long)a * sa + (long)b * sb;
+        dg = (long)da * sa + (long)db * sb;
+        dgw = sa - (long)B * sb;
+    }
+    __device__ __forceinline__ void next() {
+        a += da;
+        b += db;
+        g += dg;
+        if (b >= B) {
+            b -= B;
+            a++;
+            g += dgw;
+        }
+    }
 };
 
 // ---------------------------------------------------------------- shared-memory kernel
@@ -272,12 +318,13 @@ __device__ __forceinline__ void smem_pass(typename cplx_t<T>::t *s, int ld, int 
     const int NR = N / R;
     const int nb = nt * NR;
     const int tid = threadIdx.x, nthr = blockDim.x;
+    const unsigned mNR = magic_of((unsigned)NR), mNs = magic_of((unsigned)Ns);
     C v[K][R];
 #pragma unroll
     for (int k = 0; k < K; k++) {
         int b = tid + k * nthr;
         if (b < nb) {
-            int t = b / NR, j = b - t * NR;
+            int t = mdiv(b, mNR), j = b - t * NR;
             const C *src = s + t * ld;
 #pragma unroll
             for (int r = 0; r < R; r++) v[k][r] = src[spad(j + r * NR)];
@@ -288,8 +335,8 @@ __device__ __forceinline__ void smem_pass(typename cplx_t<T>::t *s, int ld, int 
     for (int k = 0; k < K; k++) {
         int b = tid + k * nthr;
         if (b < nb) {
-            int t = b / NR, j = b - t * NR;
-            int m = j % Ns;
+            int t = mdiv(b, mNR), j = b - t * NR;
+            int m = (Ns == 1) ? 0 : j - Ns * mdiv(j, mNs);
             if (m) {
 #pragma unroll
                 for (int r = 1; r < R; r++) v[k][r] = cmul(v[k][r], __ldg(&tp[r * Ns + m]));
@@ -319,6 +366,15 @@ __device__ __forceinline__ void smem_passes(typename cplx_t<T>::t *s, int ld, in
     for (int p = 0; p < n7; p++) { smem_pass<T, 7, EMAX>(s, ld, N, nt, Ns, tp); tp += 7 * Ns; Ns *= 7; }
 }
 
+// Walker over element (t, n) of a tile (t < nt transforms, n < L elements) of
+// a view with vector stride vs and element stride es, from global index g0
+// (transform v0, element 0).  vf: consecutive threads take consecutive
+// transforms (a = n, b = t), else consecutive elements (a = t, b = n).
+__device__ __forceinline__ void walk_tile(Walk &w, bool vf, int nt, int L, long vs, long es, long g0) {
+    if (vf) w.init(threadIdx.x, blockDim.x, nt, es, vs, g0);
+    else w.init(threadIdx.x, blockDim.x, L, vs, es, g0);
+}
+
 template <typename T, int EMAX, int MAXT>
 __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
     typedef typename cplx_t<T>::t C;
@@ -341,42 +397,45 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
         const long v0 = g * a.vpb;
         const int nt = (int)min((long)a.vpb, a.nvec - v0);
         // ---------------- load phase
+        const bool vf = a.vec_fast != 0;
+        Walk w;
         if (a.kind == K_C2C) {
             const int tot = nt * N;
-            for (int i = tid; i < tot; i += nthr) {
-                int t, n;
-                if (a.vec_fast) { t = i % nt; n = i / nt; } else { t = i / N; n = i - t * N; }
-                C c = cin.load(v0 + t, n);
+            walk_tile(w, vf, nt, N, cin.vs, cin.es, cin.off + v0 * cin.vs);
+            for (int i = tid; i < tot; i += nthr, w.next()) {
+                const int t = vf ? w.b : w.a, n = vf ? w.a : w.b;
+                C c = cin.at(w.g);
                 if (a.inv) c.y = -c.y;
                 s[t * ld + spad(n)] = c;
             }
         } else if (a.kind == K_R2C) {
             // z_n = x_{2n} + i x_{2n+1}  (c_VSIP_src/VI_rcfftmop_f_def.h:53-75)
             const int tot = nt * N;
-            for (int i = tid; i < tot; i += nthr) {
-                int t, n;
-                if (a.vec_fast) { t = i % nt; n = i / nt; } else { t = i / N; n = i - t * N; }
-                s[t * ld + spad(n)] = mk<C>(rin.load(v0 + t, 2 * n), rin.load(v0 + t, 2 * n + 1));
+            walk_tile(w, vf, nt, N, rin.vs, 2 * rin.es, rin.off + v0 * rin.vs);
+            for (int i = tid; i < tot; i += nthr, w.next()) {
+                const int t = vf ? w.b : w.a, n = vf ? w.a : w.b;
+                s[t * ld + spad(n)] = mk<C>(rin.a[rin.rst * w.g], rin.a[rin.rst * (w.g + rin.es)]);
             }
         } else {
             // C2R: raw Z_k, k <= N, then the inverse split (VI_crfftmop_f_def.h:58-110)
             const int tot = nt * (N + 1);
-            for (int i = tid; i < tot; i += nthr) {
-                int t, k;
-                if (a.vec_fast) { t = i % nt; k = i / nt; } else { t = i / (N + 1); k = i - t * (N + 1); }
-                s[t * ld + spad(k)] = cin.load(v0 + t, k);
+            walk_tile(w, vf, nt, N + 1, cin.vs, cin.es, cin.off + v0 * cin.vs);
+            for (int i = tid; i < tot; i += nthr, w.next()) {
+                const int t = vf ? w.b : w.a, k = vf ? w.a : w.b;
+                s[t * ld + spad(k)] = cin.at(w.g);
             }
             __syncthreads();
             const int half = N / 2 + 1;   // pairs (k, N-k), k = 0..N/2
             const int totp = nt * half;
+            const unsigned mh = magic_of((unsigned)half);
             for (int i = tid; i < totp; i += nthr) {
-                int t = i / half, k = i - t * half;
+                int t = mdiv(i, mh), k = i - t * half;
                 C *row = s + t * ld;
                 C f = row[spad(k)], b = row[spad(N - k)];
-                C w = thalf[k];
+                C h = thalf[k];
                 // Y_k = f + b + w.i (b - f) ... with f = Z_k, b = Z_{N-k}, w = exp(+i pi k/N)
-                C yk = mk<C>(f.x + b.x + w.y * (b.x - f.x) - w.x * (f.y + b.y),
-                             f.y - b.y - w.y * (f.y + b.y) + w.x * (f.x - b.x));
+                C yk = mk<C>(f.x + b.x + h.y * (b.x - f.x) - h.x * (f.y + b.y),
+                             f.y - b.y - h.y * (f.y + b.y) + h.x * (f.x - b.x));
                 C yn;
                 bool pair = (k != 0) && (N - k != k);
                 if (pair) {
@@ -395,20 +454,20 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
         // ---------------- store phase
         if (a.kind == K_C2C) {
             const int tot = nt * N;
-            for (int i = tid; i < tot; i += nthr) {
-                int t, n;
-                if (a.vec_fast) { t = i % nt; n = i / nt; } else { t = i / N; n = i - t * N; }
+            walk_tile(w, vf, nt, N, cout.vs, cout.es, cout.off + v0 * cout.vs);
+            for (int i = tid; i < tot; i += nthr, w.next()) {
+                const int t = vf ? w.b : w.a, n = vf ? w.a : w.b;
                 C c = s[t * ld + spad(n)];
                 if (a.inv) c.y = -c.y;
                 if (a.has_scale) c = cscale(c, a.scale);
-                cout.store(v0 + t, n, c);
+                cout.put(w.g, c);
             }
         } else if (a.kind == K_R2C) {
             // Hermitian split (VI_rcfftmop_f_def.h:79-118): X_k from Z_k and Z_{N-k} (Z_N = Z_0)
             const int tot = nt * (N + 1);
-            for (int i = tid; i < tot; i += nthr) {
-                int t, k;
-                if (a.vec_fast) { t = i % nt; k = i / nt; } else { t = i / (N + 1); k = i - t * (N + 1); }
+            walk_tile(w, vf, nt, N + 1, cout.vs, cout.es, cout.off + v0 * cout.vs);
+            for (int i = tid; i < tot; i += nthr, w.next()) {
+                const int t = vf ? w.b : w.a, k = vf ? w.a : w.b;
                 const C *row = s + t * ld;
                 C f = row[spad(k == N ? 0 : k)];
                 C b = row[spad(k == 0 ? 0 : N - k)];
@@ -416,25 +475,25 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
                     f = cscale(f, a.scale);
                     b = cscale(b, a.scale);
                 }
-                C w = thalf[k];
-                C x = mk<C>((T)0.5 * (b.x + f.x + w.x * (b.y + f.y) + w.y * (f.x - b.x)),
-                            (T)0.5 * (f.y - b.y + w.x * (b.x - f.x) + w.y * (b.y + f.y)));
-                cout.store(v0 + t, k, x);
+                C h = thalf[k];
+                C x = mk<C>((T)0.5 * (b.x + f.x + h.x * (b.y + f.y) + h.y * (f.x - b.x)),
+                            (T)0.5 * (f.y - b.y + h.x * (b.x - f.x) + h.y * (b.y + f.y)));
+                cout.put(w.g, x);
             }
         } else {
             // x_{2n} = Re y_n, x_{2n+1} = Im y_n (VI_crfftmop_f_def.h:121-124)
             const int tot = nt * N;
-            for (int i = tid; i < tot; i += nthr) {
-                int t, n;
-                if (a.vec_fast) { t = i % nt; n = i / nt; } else { t = i / N; n = i - t * N; }
+            walk_tile(w, vf, nt, N, rout.vs, 2 * rout.es, rout.off + v0 * rout.vs);
+            for (int i = tid; i < tot; i += nthr, w.next()) {
+                const int t = vf ? w.b : w.a, n = vf ? w.a : w.b;
                 C c = s[t * ld + spad(n)];
                 T re = c.x, im = -c.y;
                 if (a.has_scale) {
                     re *= a.scale;
                     im *= a.scale;
                 }
-                rout.store(v0 + t, 2 * n, re);
-                rout.store(v0 + t, 2 * n + 1, im);
+                rout.a[rout.rst * w.g] = re;
+                rout.a[rout.rst * (w.g + rout.es)] = im;
             }
         }
         __syncthreads();

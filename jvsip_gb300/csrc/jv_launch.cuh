@@ -177,7 +177,12 @@ bool launch_smem_t(const Job &j, cudaStream_t st) {
     const long elem_cap = (long)K::EMAX_L * K::MAXT_L;
     long vpb;
     if (a.vec_fast) {
+        // 16 (f32) or 8 (f64) adjacent transforms: 128-byte rows of the tile;
+        // fewer (down to one 32-byte sector) while the grid would leave SMs
+        // with under four CTAs
         vpb = (sizeof(T) == 4) ? 16 : 8;
+        const long minv = 32 / (long)sizeof(C);
+        while (vpb > minv && (j.nvec + vpb - 1) / vpb < 4L * d->sms) vpb /= 2;
         if (ld % 2 == 0) ld += 1;
     } else {
         long target = (sizeof(T) == 4) ? 2048 : 1024;
