@@ -61,7 +61,9 @@ def args():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU-baseline sample (wall seconds)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
-    ap.add_argument("--batch-gb", type=float, default=2.0, help="cfg5: bytes per buffer of the instance sequence")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="cfg5: use the cached or heuristic tiling (profiling runs: no tuner launches)")
+    ap.add_argument("--batch-gb", type=float, default=2.0, help="cfg5: bytes per buffer of the instance sequence (0: the literal 20000 instances)")
     return ap.parse_args()
 
 
@@ -232,6 +234,33 @@ def timed_calls(torch, ext, call, steps, flush=None):
     return per
 
 
+def link_time(torch, hin, hout, reps=3):
+    """ms to copy hin host->device and, at the same time, a device buffer of
+    hout's size device->host (pinned memory, two streams): the host-link bound
+    of a call that moves those bytes each way."""
+    din = torch.empty_like(hin, device="cuda")
+    dout = torch.zeros_like(hout, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def both():
+        with torch.cuda.stream(s1):
+            din.copy_(hin, non_blocking=True)
+        with torch.cuda.stream(s2):
+            hout.copy_(dout, non_blocking=True)
+
+    both()
+    torch.cuda.synchronize()
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        both()
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) * 1e3
+        best = ms if best is None else min(best, ms)
+    del din, dout
+    return best
+
+
 def line_for(a, value, ms, nbytes, dtype, launches, extra):
     peak, kind = peaks()
     d = {"metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": 1, "steps": a.steps,
@@ -347,10 +376,11 @@ def batching_workload(a, torch, J, L, ext):
     import ctypes as C
     import numpy as np
     from jvsip_gb300 import synth
-    seq = synth.batch_sequence(20000, seed=6, max_bytes=a.batch_gb * 1e9)
+    seq = synth.batch_sequence(20000, seed=6, max_bytes=(a.batch_gb * 1e9 if a.batch_gb > 0 else None))
     lit = synth.batch_sequence(20000, seed=6)
     total = sum(N * r for N, r, _, _ in seq)
     x = torch.randn(2 * total, device="cuda", generator=torch.Generator(device="cuda").manual_seed(6)).cpu().numpy()
+    torch.cuda.empty_cache()
     y = np.zeros_like(x)
     bx, by = J.CBlock(x), J.CBlock(y)
     bx.admit(True)
@@ -377,8 +407,9 @@ def batching_workload(a, torch, J, L, ext):
     lens = sorted({N for N, _, _, _ in seq})
     arr = (C.c_ulong * len(lens))(*lens)
     tune_t = time.perf_counter()
-    L.jvsip_fftm_autotune_f(len(lens), arr, 0)
-    L.jvsip_fftm_autotune_f(len(lens), arr, 1)
+    if not a.no_autotune:
+        L.jvsip_fftm_autotune_f(len(lens), arr, 0)
+        L.jvsip_fftm_autotune_f(len(lens), arr, 1)
     tune_t = time.perf_counter() - tune_t
     J.check("autotune")
     bp = L.jvsip_fftm_batch_create_f(n, P, VI, VO)
@@ -401,19 +432,20 @@ def batching_workload(a, torch, J, L, ext):
     launches = L.jvsip_gpu_kernel_launches() - n0
     ms = statistics.mean(per)
     by.sync()
-    ysave = y.copy()
+    # sampled instances: the batch's outputs (kept), then the loop's, then numpy's FP64 FFT
+    offs = np.cumsum([0] + [N * r for N, r, _, _ in seq])
+    sample = sorted({0, 1, n // 4, n // 2, (3 * n) // 4, n - 2, n - 1} & set(range(n)))
+    ysave = {k: y[2 * offs[k]:2 * offs[k + 1]].copy() for k in sample}
     lsteps = max(1, min(a.steps, 20))
     per_loop = timed_calls(torch, ext, loop, lsteps, flush)
     ms_loop = statistics.mean(per_loop)
     by.sync()
-    same = float(np.abs(ysave - y).max())
-    # accuracy of sampled instances against numpy's FP64 FFT
+    same = max(float(np.abs(ysave[k] - y[2 * offs[k]:2 * offs[k + 1]]).max()) for k in sample)
     errs = []
-    offs = np.cumsum([0] + [N * r for N, r, _, _ in seq])
-    for k in sorted({0, n // 2, n - 1}):
+    for k in sample:
         N, r, d, major = seq[k]
         xi = x[2 * offs[k]:2 * offs[k + 1]].reshape(-1, 2)
-        yi = ysave[2 * offs[k]:2 * offs[k + 1]].reshape(-1, 2)
+        yi = ysave[k].reshape(-1, 2)
         xc = (xi[:, 0] + 1j * xi[:, 1]).astype(np.complex128)
         yc = (yi[:, 0] + 1j * yi[:, 1]).astype(np.complex128)
         A = xc.reshape(r, N) if major == 0 else xc.reshape(N, r).T
@@ -424,14 +456,16 @@ def batching_workload(a, torch, J, L, ext):
     value = nbytes / (ms / 1e3) / 1e9
     loop_gbs = nbytes / (ms_loop / 1e3) / 1e9
     desc = (f"batching: {n} instances (seed 6, N log-uniform over the 175 2^a3^b5^c lengths in [64,16384], "
-            f"rows U{{1..256}}, 50/50 fwd/inv and ROW/COL) truncated at {a.batch_gb} GB per buffer; "
-            f"the literal 20000 instances are {sum(8 * N * r for N, r, _, _ in lit) / 1e9:.1f} GB per buffer")
+            f"rows U{{1..256}}, 50/50 fwd/inv and ROW/COL) "
+            + (f"truncated at {a.batch_gb} GB per buffer; " if a.batch_gb > 0 else "the literal draw, untruncated; ")
+            + f"the literal 20000 instances are {sum(8 * N * r for N, r, _, _ in lit) / 1e9:.1f} GB per buffer")
     extra = {"config": {"workload": desc, "bytes_per_step": nbytes, "instances": n,
                         "l2": "flushed between calls" if flush is not None else "inputs larger than L2"},
              "plain_loop": {"value": round(loop_gbs, 2), "unit": "GB/s", "ms_per_step": round(ms_loop, 4),
                             "calls_per_step": n},
              "batched_over_loop": round(value / loop_gbs, 2),
-             "batch_vs_loop_max_abs_diff": same, "rel_l2_vs_fp64_numpy_sampled": max(errs),
+             "batch_vs_loop_max_abs_diff_sampled": same, "rel_l2_vs_fp64_numpy_sampled": max(errs),
+             "sampled_instances": len(sample),
              "autotune_s": round(tune_t, 2), "autotune_entries": int(L.jvsip_fftm_autotune_entries())}
     print(json.dumps(line_for(a, value, ms, nbytes, "f32", launches, extra)), flush=True)
 
@@ -537,10 +571,18 @@ def main():
             ems = float(t.item())
         ye_np = ye.numpy()
         k = 2 * N * min(64, M)
+        diff = float(np.abs(ye_np[:k] - y_np[:k]).max())
+        link_ms = link_time(torch, xe, ye)  # overwrites ye
         e2e = {"value": round(nbytes * world / (ems / 1e3) / 1e9, 2), "unit": "GB/s",
                "h2d_bytes_per_step": n2 * 4, "d2h_bytes_per_step": n2 * 4, "ms_per_step": round(ems, 3),
                "path": "vsip_ccfftmop_f on pinned, non-admitted user blocks (staged inside the call)",
-               "max_abs_diff_vs_resident": float(np.abs(ye_np[:k] - y_np[:k]).max())}
+               "max_abs_diff_vs_resident": diff,
+               "link": {"ms_both_directions": round(link_ms, 3),
+                        "gbs_each_way": round(n2 * 4 / (link_ms / 1e3) / 1e9, 1),
+                        "roofline_value": round(nbytes / (link_ms / 1e3) / 1e9, 2),
+                        "frac": round(link_ms / ems, 4),
+                        "how": "the same bytes copied host->device and device->host at once on two streams "
+                               "(pinned memory), no transform: the host link bounds the e2e path"}}
         for v in (vxe, vye):
             v.destroy()
         for b in (bxe, bye):

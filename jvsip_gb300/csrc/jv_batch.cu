@@ -63,12 +63,7 @@ __device__ __forceinline__ void batch_tile(const TileDesc &d, float2 *s) {
     const bool vf = d.vec_fast != 0;
     Walk w;
     walk_tile(w, vf, nt, N, cin.vs, cin.es, cin.off + d.v0 * cin.vs);
-    for (int i = tid; i < tot; i += nthr, w.next()) {
-        const int t = vf ? w.b : w.a, n = vf ? w.a : w.b;
-        float2 c = cin.at(w.g);
-        if (d.inv) c.y = -c.y;
-        s[t * ld + spad(n)] = c;
-    }
+    tile_load<8>(w, vf, tot, s, ld, d.inv != 0, [&](long g) { return cin.at(g); });
     __syncthreads();
     smem_passes<float, BEMAX>(s, ld, N, nt, d.n8, d.n4, d.n2, d.n3, d.n5, d.n7, d.twg);
     walk_tile(w, vf, nt, N, cout.vs, cout.es, cout.off + d.v0 * cout.vs);

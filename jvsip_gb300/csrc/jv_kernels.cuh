@@ -375,6 +375,34 @@ __device__ __forceinline__ void walk_tile(Walk &w, bool vf, int nt, int L, long 
     else w.init(threadIdx.x, blockDim.x, L, vs, es, g0);
 }
 
+// Copies tot tile elements from global to shared memory (row pitch ld, padded
+// index) with LB loads in flight per thread: LB addresses are walked and their
+// loads issued before any of the values is stored.  get(g) reads the element
+// at global index g; conj negates the imaginary parts.
+template <int LB, typename C, typename Get>
+__device__ __forceinline__ void tile_load(Walk &w, bool vf, int tot, C *s, int ld, bool conj, Get get) {
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    for (int i0 = tid; i0 < tot; i0 += LB * nthr) {
+        C c[LB];
+        int o[LB];
+#pragma unroll
+        for (int u = 0; u < LB; u++) {
+            const int t = vf ? w.b : w.a, n = vf ? w.a : w.b;
+            o[u] = t * ld + spad(n);
+            if (i0 + u * nthr < tot) c[u] = get(w.g);
+            w.next();
+        }
+#pragma unroll
+        for (int u = 0; u < LB; u++) {
+            if (i0 + u * nthr < tot) {
+                C v = c[u];
+                if (conj) v.y = -v.y;
+                s[o[u]] = v;
+            }
+        }
+    }
+}
+
 template <typename T, int EMAX, int MAXT>
 __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
     typedef typename cplx_t<T>::t C;
@@ -398,32 +426,20 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
         const int nt = (int)min((long)a.vpb, a.nvec - v0);
         // ---------------- load phase
         const bool vf = a.vec_fast != 0;
+        constexpr int LB = (sizeof(T) == 4 && EMAX <= 8) ? 8 : 4;  // loads in flight per thread
         Walk w;
         if (a.kind == K_C2C) {
-            const int tot = nt * N;
             walk_tile(w, vf, nt, N, cin.vs, cin.es, cin.off + v0 * cin.vs);
-            for (int i = tid; i < tot; i += nthr, w.next()) {
-                const int t = vf ? w.b : w.a, n = vf ? w.a : w.b;
-                C c = cin.at(w.g);
-                if (a.inv) c.y = -c.y;
-                s[t * ld + spad(n)] = c;
-            }
+            tile_load<LB>(w, vf, nt * N, s, ld, a.inv != 0, [&](long g) { return cin.at(g); });
         } else if (a.kind == K_R2C) {
             // z_n = x_{2n} + i x_{2n+1}  (c_VSIP_src/VI_rcfftmop_f_def.h:53-75)
-            const int tot = nt * N;
             walk_tile(w, vf, nt, N, rin.vs, 2 * rin.es, rin.off + v0 * rin.vs);
-            for (int i = tid; i < tot; i += nthr, w.next()) {
-                const int t = vf ? w.b : w.a, n = vf ? w.a : w.b;
-                s[t * ld + spad(n)] = mk<C>(rin.a[rin.rst * w.g], rin.a[rin.rst * (w.g + rin.es)]);
-            }
+            tile_load<LB>(w, vf, nt * N, s, ld, false,
+                          [&](long g) { return mk<C>(rin.a[rin.rst * g], rin.a[rin.rst * (g + rin.es)]); });
         } else {
             // C2R: raw Z_k, k <= N, then the inverse split (VI_crfftmop_f_def.h:58-110)
-            const int tot = nt * (N + 1);
             walk_tile(w, vf, nt, N + 1, cin.vs, cin.es, cin.off + v0 * cin.vs);
-            for (int i = tid; i < tot; i += nthr, w.next()) {
-                const int t = vf ? w.b : w.a, k = vf ? w.a : w.b;
-                s[t * ld + spad(k)] = cin.at(w.g);
-            }
+            tile_load<LB>(w, vf, nt * (N + 1), s, ld, false, [&](long g) { return cin.at(g); });
             __syncthreads();
             const int half = N / 2 + 1;   // pairs (k, N-k), k = 0..N/2
             const int totp = nt * half;
