@@ -30,9 +30,12 @@ struct TileDesc {
     long in_off, in_es, in_vs;
     long out_off, out_es, out_vs;
     const float2 *twg;  // per-pass [r][m] tables of the call's plan
+    const uint4 *pc;    // per-pass constants of the plan's schedule
+    unsigned long long passes;  // pass counts per codelet (pass_count)
+    unsigned mnt;       // multiply-high magic of nt
     long v0;
     int N, nt, ld;
-    unsigned char n8, n4, n2, n3, n5, n7, inv, vec_fast;
+    unsigned char inv, vec_fast;
     int has_scale;
     float scale;
 };
@@ -41,40 +44,29 @@ constexpr int BT = 1024;      // threads of a batch CTA
 constexpr int BEMAX = 16;     // complex values a thread keeps per pass: tiles of <= 16384 points
 
 __device__ __forceinline__ void batch_tile(const TileDesc &d, float2 *s) {
-    const int N = d.N, ld = d.ld, nt = d.nt;
-    const int tid = threadIdx.x, nthr = blockDim.x;
-    CAcc<float> cin;
-    cin.re = d.in;
-    cin.im = d.in + 1;
-    cin.cst = 2;
-    cin.off = d.in_off;
-    cin.es = d.in_es;
-    cin.vs = d.in_vs;
-    cin.vec = true;
-    CSto<float> cout;
-    cout.re = d.out;
-    cout.im = d.out + 1;
-    cout.cst = 2;
-    cout.off = d.out_off;
-    cout.es = d.out_es;
-    cout.vs = d.out_vs;
-    cout.vec = true;
-    const int tot = nt * N;
-    const bool vf = d.vec_fast != 0;
-    Walk w;
-    walk_tile(w, vf, nt, N, cin.vs, cin.es, cin.off + d.v0 * cin.vs);
-    tile_load<8>(w, vf, tot, s, ld, d.inv != 0, [&](long g) { return cin.at(g); });
-    __syncthreads();
-    smem_passes<float, BEMAX>(s, ld, N, nt, d.n8, d.n4, d.n2, d.n3, d.n5, d.n7, d.twg);
-    walk_tile(w, vf, nt, N, cout.vs, cout.es, cout.off + d.v0 * cout.vs);
-    for (int i = tid; i < tot; i += nthr, w.next()) {
-        const int t = vf ? w.b : w.a, n = vf ? w.a : w.b;
-        float2 c = s[t * ld + spad(n)];
-        if (d.inv) c.y = -c.y;
-        if (d.has_scale) c = cscale(c, d.scale);
-        cout.put(w.g, c);
-    }
-    __syncthreads();
+    TileIO<float> io;
+    io.in.re = d.in;
+    io.in.im = d.in + 1;
+    io.in.cst = 2;
+    io.in.off = d.in_off;
+    io.in.es = d.in_es;
+    io.in.vs = d.in_vs;
+    io.in.vec = true;
+    io.out.re = d.out;
+    io.out.im = d.out + 1;
+    io.out.cst = 2;
+    io.out.off = d.out_off;
+    io.out.es = d.out_es;
+    io.out.vs = d.out_vs;
+    io.out.vec = true;
+    io.gin = d.in_off + d.v0 * d.in_vs;
+    io.gout = d.out_off + d.v0 * d.out_vs;
+    io.vf = d.vec_fast != 0;
+    io.conj = d.inv != 0;
+    io.has_scale = d.has_scale != 0;
+    io.scale = d.scale;
+    io.mnt = d.mnt;
+    c2c_tile<float, BEMAX>(s, d.ld, d.nt, d.passes, d.twg, d.pc, io);
 }
 
 // One launch over the whole queue: CTA b takes descriptor b.  The queue is
@@ -121,7 +113,7 @@ static bool build_tiles(size_t n, const vsip_fftm_f *const plans[], const vsip_c
             set_error(E_ARG, "batch: every plan must be a single-precision c2c plan");
             return false;
         }
-        if (!p->smooth || !p->d_twg || p->MN > BEMAX * BT) {
+        if (!p->smooth || !p->d_twg || !p->d_pc || p->radix.empty() || p->MN > BEMAX * BT) {
             set_error(E_UNSUPPORTED, "batch: lengths must be 2^a 3^b 5^c 7^d and at most 16384");
             return false;
         }
@@ -178,16 +170,11 @@ static bool build_tiles(size_t n, const vsip_fftm_f *const plans[], const vsip_c
             return false;
         }
         t.twg = (const float2 *)p->d_twg;
+        t.pc = (const uint4 *)p->d_pc;
         t.N = (int)N;
-        for (int r : p->radix) {
-            switch (r) {
-                case 8: t.n8++; break;
-                case 4: t.n4++; break;
-                case 2: t.n2++; break;
-                case 3: t.n3++; break;
-                case 5: t.n5++; break;
-                case 7: t.n7++; break;
-            }
+        if (!pack_passes(p->radix, &t.passes)) {
+            set_error(E_UNSUPPORTED, "batch: pass schedule outside the codelets");
+            return false;
         }
         t.inv = (p->dir == 1) ? 1 : 0;
         t.has_scale = (p->scale != 1.0) ? 1 : 0;
@@ -197,11 +184,18 @@ static bool build_tiles(size_t n, const vsip_fftm_f *const plans[], const vsip_c
         t.vec_fast = (vf_in || vf_out) ? 1 : 0;
         t.ld = (int)tile_ld(N, t.vec_fast);
         long per = batch_fft_per_tile(N, t.vec_fast, nv);
+        // every pass of the tile must fit the CTA: a thread holds
+        // pass_k(BEMAX, R) butterflies of radix R (the plan's schedule fits
+        // one transform by construction)
+        long min_pts = BEMAX;
+        for (int r : p->radix) min_pts = std::min(min_pts, (long)r * pass_k(BEMAX, r));
+        while (per > 1 && per * N > (long)BT * min_pts) per--;
         while (per > 1 && per * (long)t.ld * 8 > (long)d->smem_optin - 512) per--;
         for (long v0 = 0; v0 < nv; v0 += per) {
             TileDesc u = t;
             u.v0 = v0;
             u.nt = (int)std::min(per, nv - v0);
+            u.mnt = magic_host((unsigned long)u.nt);
             bb.tiles.push_back(u);
             bb.smem = std::max(bb.smem, (size_t)u.nt * u.ld * 8);
         }

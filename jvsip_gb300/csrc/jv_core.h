@@ -102,6 +102,7 @@ struct Job {
     const void *thalf = nullptr;  // R2C/C2R table exp(-+ i pi k/MN), k <= MN
     const void *twp = nullptr;    // per-pass twiddle tables of the specialised kernel (or null)
     const void *twg = nullptr;    // per-pass twiddle tables of the general kernel's schedule
+    const void *pc = nullptr;     // per-pass constants of that schedule (PassConst)
     int npass = 0;
     int radix[40];
     int form = 0;        // JVSIP_FORM_* of the plan
@@ -110,6 +111,8 @@ struct Job {
 // Kernel entry points (defined in the kernel translation units).
 bool launch_smem_f32(const Job &j, cudaStream_t s);
 bool launch_smem_f64(const Job &j, cudaStream_t s);
+bool launch_smem_real_f32(const Job &j, cudaStream_t s);  // R2C / C2R instances
+bool launch_smem_real_f64(const Job &j, cudaStream_t s);
 bool launch_global_f32(const Job &j, cudaStream_t s);
 bool launch_global_f64(const Job &j, cudaStream_t s);
 bool launch_fast_f32(const Job &j, cudaStream_t s);   // specialised kernels; false when none fits
@@ -136,7 +139,8 @@ struct Plan {
     void *d_tw = nullptr;     // forward twiddles, MN entries
     void *d_thalf = nullptr;  // half-angle table, MN+1 entries (real transforms)
     void *d_twp = nullptr;    // per-pass [r][m] twiddle tables of the specialised kernel
-    void *d_twg = nullptr;    // per-pass [r][m] twiddle tables of the general kernel (radix <= 8 schedule)
+    void *d_twg = nullptr;    // per-pass [r][m] twiddle tables of the general kernel's schedule
+    void *d_pc = nullptr;     // per-pass constants of that schedule (PassConst, one per pass)
     std::vector<unsigned long> jofk;  // reference digit-reversal map (kept for parity checks)
     std::mutex mu;            // the plan is used by one call at a time
 };
@@ -145,7 +149,25 @@ Plan *plan_of(const void *vsip_plan);   // ext_fftm_obj of a vsip_fftm_* (nullpt
 
 // factorisation of the reference (c_VSIP_src/VI_nuV.h:22-136); returns the stage count
 unsigned long ref_factor(unsigned long N, unsigned long *pn, unsigned long *p0, unsigned long *pF);
-// device pass radices for length N: codelets 16, 8, 4, 2, 5, 3, 7, then any other prime
-std::vector<int> pass_radices(long N, bool *smooth);
+// Constants of one pass of the general kernel's schedule: NR = N/R, the
+// multiply-high magic of NR and of Ns (product of the earlier radices), Ns.
+struct PassConst {
+    unsigned NR, mNR, Ns, mNs;
+};
+// floor(x / d) == __umulhi(x, m) for x * d < 2^32 with m = ceil(2^32 / d); 0 encodes d = 1
+inline unsigned magic_host(unsigned long d) { return d <= 1 ? 0u : (unsigned)(0xFFFFFFFFul / d + 1ul); }
+// Butterflies a thread keeps per radix-R pass of the general kernel sized for
+// EMAX points: ceil(EMAX/R) for the prime-power codelets (R <= 8), one (or
+// EMAX/R) for the composite ones, whose registers are already R points.
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+constexpr int pass_k(int EMAX, int R) { return R <= 8 ? (EMAX + R - 1) / R : (EMAX >= R ? EMAX / R : 1); }
+// Radix codelets of the general kernel, in the order of its pass loops.
+constexpr int kRadices = 13;
+constexpr int kRadixList[kRadices] = {16, 15, 14, 12, 10, 9, 8, 7, 6, 5, 4, 3, 2};
+// device pass radices for length N: for 2^a 3^b 5^c 7^d the fewest passes of
+// the codelets above (largest first), else radix 8/4/2, 3, 5, 7, then any other prime
+std::vector<int> pass_radices(long N, bool *smooth, long maxt);  // maxt: threads per CTA of the shared-memory kernel
 
 }  // namespace jv

@@ -245,10 +245,12 @@ static bool run_job(Job &j, cudaStream_t st) {
     if (j.nvec <= 0 || j.N <= 0) return true;
     long lim = smem_max_len(j.prec, j.kind);
     bool smooth = true;
-    for (int i = 0; i < j.npass; i++)
-        if (j.radix[i] != 2 && j.radix[i] != 3 && j.radix[i] != 4 && j.radix[i] != 5 && j.radix[i] != 7 &&
-            j.radix[i] != 8)
-            smooth = false;
+    for (int i = 0; i < j.npass; i++) {
+        bool codelet = false;
+        for (int r = 0; r < kRadices; r++) codelet = codelet || (j.radix[i] == kRadixList[r]);
+        if (!codelet) smooth = false;
+    }
+    if (!j.twg || !j.pc) smooth = false;
     long need = j.N + (j.kind == K_C2R ? 1 : 0);
     if (j.form == JVSIP_FORM_SPLIT_BF16 || j.form == JVSIP_FORM_SPLIT_FP16) {
         if (launch_split_f32(j, st)) return jvsip_gpu_last_error() == 0;
@@ -284,6 +286,7 @@ static void fill_job(Job &j, const Plan *p, int kind) {
     j.thalf = p->d_thalf;
     j.twp = p->d_twp;
     j.twg = p->d_twg;
+    j.pc = p->d_pc;
     j.form = p->form;
     j.npass = (int)p->radix.size();
     for (int i = 0; i < j.npass && i < 40; i++) j.radix[i] = p->radix[i];

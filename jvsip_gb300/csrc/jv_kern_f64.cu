@@ -1,8 +1,13 @@
-// jv_kern_f64.cu -- double-precision instances of the general kernels.
+// jv_kern_f64.cu -- double-precision instances of the general kernels (c2c
+// shared-memory kernel, global-memory path, capacity query); the real
+// transforms' shared-memory kernels are in jv_kern_f64r.cu.
 #include "jv_launch.cuh"
 
 namespace jv {
-bool launch_smem_f64(const Job &j, cudaStream_t s) { return launch_smem_t<double>(j, s); }
+bool launch_smem_f64(const Job &j, cudaStream_t s) {
+    if (j.kind == K_C2C) return launch_smem_t<double, K_C2C>(j, s);
+    return launch_smem_real_f64(j, s);
+}
 bool launch_global_f64(const Job &j, cudaStream_t s) { return launch_global_t<double>(j, s); }
 long smem_max_len_f64(int kind) { return smem_len_limit<double>(kind); }
 }  // namespace jv

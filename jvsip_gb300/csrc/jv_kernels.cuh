@@ -2,7 +2,8 @@
 // the small-DFT codelets, view addressing, and the two general kernels
 //
 //   k_smem : a whole transform (or several) per CTA, resident in shared
-//            memory; self-sorting (Stockham) radix passes 2,3,4,5,7,8,16,
+//            memory; self-sorting (Stockham) radix passes with the codelets
+//            2, 3, 4, 5, 6, 7, 8, 9, 10, 12, 14, 15, 16,
 //            each thread holding its butterflies in registers across the
 //            pass; R2C packing/Hermitian split and C2R un-split are fused into
 //            the load and store phases.
@@ -189,6 +190,98 @@ template <typename C> struct Dft<C, 7> {
     }
 };
 
+// ---- composite codelets R = P*Q (6, 9, 10, 12, 14, 15) from the prime-power
+// ones, with their internal twiddles exp(-2 pi i e/R) evaluated by the compiler
+// (Taylor series on an exactly reduced angle, |x| <= pi/4, in double).
+namespace cx {
+constexpr double kPi = 3.14159265358979323846264338327950288;
+constexpr double sin_small(double x) {
+    double x2 = x * x, term = x, sum = x;
+    for (int k = 1; k < 14; k++) {
+        term *= -x2 / ((2.0 * k) * (2.0 * k + 1.0));
+        sum += term;
+    }
+    return sum;
+}
+constexpr double cos_small(double x) {
+    double x2 = x * x, term = 1.0, sum = 1.0;
+    for (int k = 1; k < 14; k++) {
+        term *= -x2 / ((2.0 * k - 1.0) * (2.0 * k));
+        sum += term;
+    }
+    return sum;
+}
+// cos and sin of 2 pi e/R: quadrant q = floor(4e/R), remainder r/R of a
+// quarter turn, folded to an angle of at most pi/4
+constexpr double root_cs(int R, int e, bool want_sin) {
+    e %= R;
+    const int q = (4 * e) / R, r = 4 * e - q * R;
+    const bool fold = 2 * r > R;
+    const double x = (kPi / 2.0) * (double)(fold ? R - r : r) / (double)R;
+    double c = fold ? sin_small(x) : cos_small(x), s = fold ? cos_small(x) : sin_small(x);
+    double cq = c, sq = s;  // rotate by q quarter turns
+    if (q == 1) { cq = -s; sq = c; }
+    if (q == 2) { cq = -c; sq = -s; }
+    if (q == 3) { cq = s; sq = -c; }
+    return want_sin ? sq : cq;
+}
+}  // namespace cx
+
+template <int R, int E> struct Root {  // exp(-2 pi i E/R)
+    static constexpr double c = cx::root_cs(R, E, false);
+    static constexpr double s = -cx::root_cs(R, E, true);
+};
+
+template <typename C, int R, int E>
+__device__ __forceinline__ C cmul_root(C a) {
+    typedef decltype(C::x) T;
+    const T c = (T)Root<R, E>::c, s = (T)Root<R, E>::s;
+    return mk<C>(a.x * c - a.y * s, a.x * s + a.y * c);
+}
+
+// a[n2][k1] *= exp(-2 pi i n2 k1/R) for every index I = n2*P + k1 >= I0
+template <typename C, int R, int P, int Q, int I>
+struct PQTwiddle {
+    static __device__ __forceinline__ void run(C (&a)[Q][P]) {
+        constexpr int n2 = I / P, k1 = I % P;
+        if constexpr (n2 * k1 != 0) a[n2][k1] = cmul_root<C, R, n2 * k1>(a[n2][k1]);
+        if constexpr (I + 1 < P * Q) PQTwiddle<C, R, P, Q, I + 1>::run(a);
+    }
+};
+
+// R = P*Q points: n = Q n1 + n2, k = k1 + P k2;
+// X[k1 + P k2] = sum_n2 w_Q^(n2 k2) w_R^(n2 k1) sum_n1 x[Q n1 + n2] w_P^(n1 k1)
+template <typename C, int P, int Q> struct DftPQ {
+    static __device__ __forceinline__ void run(C *v) {
+        C a[Q][P];
+#pragma unroll
+        for (int n2 = 0; n2 < Q; n2++) {
+            C t[P];
+#pragma unroll
+            for (int n1 = 0; n1 < P; n1++) t[n1] = v[Q * n1 + n2];
+            Dft<C, P>::run(t);
+#pragma unroll
+            for (int k1 = 0; k1 < P; k1++) a[n2][k1] = t[k1];
+        }
+        PQTwiddle<C, P * Q, P, Q, 0>::run(a);
+#pragma unroll
+        for (int k1 = 0; k1 < P; k1++) {
+            C t[Q];
+#pragma unroll
+            for (int n2 = 0; n2 < Q; n2++) t[n2] = a[n2][k1];
+            Dft<C, Q>::run(t);
+#pragma unroll
+            for (int k2 = 0; k2 < Q; k2++) v[k1 + P * k2] = t[k2];
+        }
+    }
+};
+template <typename C> struct Dft<C, 6> : DftPQ<C, 2, 3> {};
+template <typename C> struct Dft<C, 9> : DftPQ<C, 3, 3> {};
+template <typename C> struct Dft<C, 10> : DftPQ<C, 2, 5> {};
+template <typename C> struct Dft<C, 12> : DftPQ<C, 4, 3> {};
+template <typename C> struct Dft<C, 14> : DftPQ<C, 2, 7> {};
+template <typename C> struct Dft<C, 15> : DftPQ<C, 3, 5> {};
+
 // ---------------------------------------------------------------- view access
 // Complex element (v, n) of a CView; `conj` negates the imaginary part.
 template <typename T> struct CAcc {
@@ -248,6 +341,20 @@ template <typename T> struct RSto {
 __device__ __forceinline__ unsigned magic_of(unsigned d) { return d <= 1 ? 0u : 0xFFFFFFFFu / d + 1u; }
 __device__ __forceinline__ int mdiv(int x, unsigned m) { return m ? (int)__umulhi((unsigned)x, m) : x; }
 
+// Walker constants computed at launch for a grid of width B and blockDim threads.
+struct WalkConst {
+    int B, da, db;
+    unsigned mB;
+};
+inline WalkConst walk_const(long B, long nthr) {
+    WalkConst c;
+    c.B = (int)B;
+    c.da = (int)(nthr / B);
+    c.db = (int)(nthr % B);
+    c.mB = magic_host((unsigned long)B);
+    return c;
+}
+
 // Walks i = i0, i0 + step, ... over an A x B grid (i = a*B + b, b fastest)
 // keeping the global element index g = g0 + a*sa + b*sb up to date with adds:
 // one division per thread at the start, none per element.
@@ -260,6 +367,18 @@ struct Walk {
         b = i0 - a * B;
         da = step / B;
         db = step - da * B;
+        g = g0 + (long)a * sa + (long)b * sb;
+        dg = (long)da * sa + (long)db * sb;
+        dgw = sa - (long)B * sb;
+    }
+    // the same from launch-time constants (B, nthr / B, nthr % B, magic of B):
+    // no division at all
+    __device__ __forceinline__ void init_c(const WalkConst c, long sa, long sb, long g0) {
+        B = c.B;
+        a = mdiv((int)threadIdx.x, c.mB);
+        b = (int)threadIdx.x - a * B;
+        da = c.da;
+        db = c.db;
         g = g0 + (long)a * sa + (long)b * sb;
         dg = (long)da * sa + (long)db * sb;
         dgw = sa - (long)B * sb;
@@ -288,10 +407,10 @@ template <typename T> struct SmemArgs {
     int has_scale;
     T scale;
     int vec_fast;     // global load/store mapping: consecutive threads -> consecutive transforms
-    // pass schedule: n8 radix-8 passes, then n4 radix-4, n2 radix-2, n3 radix-3,
-    // n5 radix-5 and n7 radix-7 passes (a loop per radix keeps register
-    // lifetimes of different codelets apart)
-    int n8, n4, n2, n3, n5, n7;
+    unsigned long long passes;  // pass counts per codelet (pass_count)
+    const uint4 *pc;  // per-pass constants of the schedule (NR, magic NR, Ns, magic Ns)
+    unsigned mvpb;    // multiply-high magic of vpb
+    WalkConst win, wout;  // load / store walker constants for full tiles of vpb transforms
     CAcc<T> cin;
     CSto<T> cout;
     RAcc<T> rin;
@@ -308,17 +427,23 @@ template <typename T> struct SmemArgs {
 // pass needs ceil(EMAX/R) * blockDim >= transforms * N/R.
 __device__ __forceinline__ int spad(int i) { return i + (i >> 4); }
 
+// pass counts per codelet (order of kRadixList), 4 bits each
+__host__ __device__ __forceinline__ int pass_count(unsigned long long packed, int i) {
+    return (int)((packed >> (4 * i)) & 15ull);
+}
+
 template <typename T, int R, int EMAX>
-__device__ __forceinline__ void smem_pass(typename cplx_t<T>::t *s, int ld, int N, int nt, int Ns,
-                                          const typename cplx_t<T>::t *__restrict__ tp) {
+__device__ __forceinline__ void smem_pass(typename cplx_t<T>::t *s, int ld, int nt, int Ns,
+                                          const typename cplx_t<T>::t *__restrict__ tp, const uint4 pc) {
     // tp: this pass's twiddles, entry r*Ns + m = exp(-2 pi i r m/(Ns R)), so the
-    // threads of a warp (consecutive m) read consecutive entries
+    // threads of a warp (consecutive m) read consecutive entries; pc: NR = N/R,
+    // the multiply-high magic numbers of NR and Ns
     typedef typename cplx_t<T>::t C;
-    constexpr int K = (EMAX + R - 1) / R;
-    const int NR = N / R;
+    constexpr int K = pass_k(EMAX, R);
+    const int NR = (int)pc.x;
     const int nb = nt * NR;
     const int tid = threadIdx.x, nthr = blockDim.x;
-    const unsigned mNR = magic_of((unsigned)NR), mNs = magic_of((unsigned)Ns);
+    const unsigned mNR = pc.y, mNs = pc.w;
     C v[K][R];
 #pragma unroll
     for (int k = 0; k < K; k++) {
@@ -351,28 +476,244 @@ __device__ __forceinline__ void smem_pass(typename cplx_t<T>::t *s, int ld, int 
     __syncthreads();
 }
 
+// The plan's schedule: `packed` pass counts per codelet in the order of
+// kRadixList (the order of the plan's per-pass twiddle tables twg and pass
+// constants pc).  One loop per codelet keeps the codelets' register lifetimes
+// apart.
 template <typename T, int EMAX>
-__device__ __forceinline__ void smem_passes(typename cplx_t<T>::t *s, int ld, int N, int nt, int n8, int n4,
-                                            int n2, int n3, int n5, int n7,
-                                            const typename cplx_t<T>::t *__restrict__ twg) {
-    // passes run in the order of the plan's per-pass tables: 8s, 4, 2, 3s, 5s, 7s
-    int Ns = 1;
+__device__ __forceinline__ void smem_passes_from(typename cplx_t<T>::t *s, int ld, int nt, unsigned long long packed,
+                                                 const typename cplx_t<T>::t *__restrict__ &tp,
+                                                 const uint4 *__restrict__ pc, int &Ns, int &p);
+
+template <typename T, int EMAX>
+__device__ __forceinline__ void smem_passes(typename cplx_t<T>::t *s, int ld, int nt, unsigned long long packed,
+                                            const typename cplx_t<T>::t *__restrict__ twg,
+                                            const uint4 *__restrict__ pc) {
+    int Ns = 1, p = 0;
     const typename cplx_t<T>::t *tp = twg;
-    for (int p = 0; p < n8; p++) { smem_pass<T, 8, EMAX>(s, ld, N, nt, Ns, tp); tp += 8 * Ns; Ns *= 8; }
-    for (int p = 0; p < n4; p++) { smem_pass<T, 4, EMAX>(s, ld, N, nt, Ns, tp); tp += 4 * Ns; Ns *= 4; }
-    for (int p = 0; p < n2; p++) { smem_pass<T, 2, EMAX>(s, ld, N, nt, Ns, tp); tp += 2 * Ns; Ns *= 2; }
-    for (int p = 0; p < n3; p++) { smem_pass<T, 3, EMAX>(s, ld, N, nt, Ns, tp); tp += 3 * Ns; Ns *= 3; }
-    for (int p = 0; p < n5; p++) { smem_pass<T, 5, EMAX>(s, ld, N, nt, Ns, tp); tp += 5 * Ns; Ns *= 5; }
-    for (int p = 0; p < n7; p++) { smem_pass<T, 7, EMAX>(s, ld, N, nt, Ns, tp); tp += 7 * Ns; Ns *= 7; }
+    smem_passes_from<T, EMAX>(s, ld, nt, packed, tp, pc, Ns, p);
+}
+
+// ---------------------------------------------------------------- fused first / last passes (c2c)
+// A c2c tile's first radix pass reads the view in global memory directly and
+// its last pass writes the view directly, so a tile crosses shared memory only
+// between passes.  Butterfly b of the tile maps to (transform t, index j):
+// j fastest for row tiles (consecutive threads read consecutive elements),
+// t fastest for column tiles (consecutive threads read adjacent transforms).
+template <typename T> struct TileIO {
+    CAcc<T> in;
+    CSto<T> out;
+    long gin, gout;  // global index of element 0 of the tile's first transform
+    bool vf;         // t-fastest mapping
+    bool conj;       // inverse: conjugate on load and on store
+    bool has_scale;
+    T scale;
+    unsigned mnt;    // multiply-high magic of the tile's transform count
+};
+
+__device__ __forceinline__ void tile_tj(int b, bool vf, int nt, unsigned mnt, int NR, unsigned mNR, int &t, int &j) {
+    if (vf) {
+        j = mdiv(b, mnt);
+        t = b - j * nt;
+    } else {
+        t = mdiv(b, mNR);
+        j = b - t * NR;
+    }
+}
+
+// First pass (Ns = 1, no twiddle) from global memory; to shared memory, or,
+// for a one-pass schedule (LAST), straight back to global memory.
+template <typename T, int R, int EMAX, bool LAST>
+__device__ __forceinline__ void pass_first(typename cplx_t<T>::t *s, int ld, int nt, const uint4 pc,
+                                           const TileIO<T> &io) {
+    typedef typename cplx_t<T>::t C;
+    constexpr int K = pass_k(EMAX, R);
+    const int NR = (int)pc.x, nb = nt * NR;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    C v[K][R];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const int b = tid + k * nthr;
+        if (b < nb) {
+            int t, j;
+            tile_tj(b, io.vf, nt, io.mnt, NR, pc.y, t, j);
+            const long g = io.gin + (long)t * io.in.vs + (long)j * io.in.es, st = (long)NR * io.in.es;
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                C c = io.in.at(g + r * st);
+                if (io.conj) c.y = -c.y;
+                v[k][r] = c;
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const int b = tid + k * nthr;
+        if (b < nb) {
+            int t, j;
+            tile_tj(b, io.vf, nt, io.mnt, NR, pc.y, t, j);
+            Dft<C, R>::run(v[k]);
+            if (LAST) {
+                // one pass: N = R, j = 0, output element r
+                const long g = io.gout + (long)t * io.out.vs;
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    C c = v[k][r];
+                    if (io.conj) c.y = -c.y;
+                    if (io.has_scale) c = cscale(c, io.scale);
+                    io.out.put(g + (long)r * io.out.es, c);
+                }
+            } else {
+                C *dst = s + t * ld;
+#pragma unroll
+                for (int r = 0; r < R; r++) dst[spad(j * R + r)] = v[k][r];
+            }
+        }
+    }
+    if (!LAST) __syncthreads();
+}
+
+// Last pass (Ns = N/R, so m = j) from shared memory to global memory.
+template <typename T, int R, int EMAX>
+__device__ __forceinline__ void pass_last(const typename cplx_t<T>::t *s, int ld, int nt, int Ns,
+                                          const typename cplx_t<T>::t *__restrict__ tp, const uint4 pc,
+                                          const TileIO<T> &io) {
+    typedef typename cplx_t<T>::t C;
+    constexpr int K = pass_k(EMAX, R);
+    const int NR = (int)pc.x, nb = nt * NR;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    C v[K][R];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const int b = tid + k * nthr;
+        if (b < nb) {
+            int t, j;
+            tile_tj(b, io.vf, nt, io.mnt, NR, pc.y, t, j);
+            const C *src = s + t * ld;
+#pragma unroll
+            for (int r = 0; r < R; r++) v[k][r] = src[spad(j + r * NR)];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const int b = tid + k * nthr;
+        if (b < nb) {
+            int t, j;
+            tile_tj(b, io.vf, nt, io.mnt, NR, pc.y, t, j);
+            if (j) {
+#pragma unroll
+                for (int r = 1; r < R; r++) v[k][r] = cmul(v[k][r], __ldg(&tp[r * Ns + j]));
+            }
+            Dft<C, R>::run(v[k]);
+            const long g = io.gout + (long)t * io.out.vs + (long)j * io.out.es, st = (long)Ns * io.out.es;
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                C c = v[k][r];
+                if (io.conj) c.y = -c.y;
+                if (io.has_scale) c = cscale(c, io.scale);
+                io.out.put(g + r * st, c);
+            }
+        }
+    }
+}
+
+#define JV_RADIX_SWITCH(I, CALL) \
+    switch (I) {                 \
+        case 0: CALL(16); break; \
+        case 1: CALL(15); break; \
+        case 2: CALL(14); break; \
+        case 3: CALL(12); break; \
+        case 4: CALL(10); break; \
+        case 5: CALL(9); break;  \
+        case 6: CALL(8); break;  \
+        case 7: CALL(7); break;  \
+        case 8: CALL(6); break;  \
+        case 9: CALL(5); break;  \
+        case 10: CALL(4); break; \
+        case 11: CALL(3); break; \
+        default: CALL(2); break; \
+    }
+
+// A whole c2c tile: global -> passes -> global.  The schedule must have at
+// least one pass.
+template <typename T, int EMAX>
+__device__ __forceinline__ void c2c_tile(typename cplx_t<T>::t *s, int ld, int nt, unsigned long long packed,
+                                         const typename cplx_t<T>::t *__restrict__ twg,
+                                         const uint4 *__restrict__ pc, const TileIO<T> &io) {
+    typedef typename cplx_t<T>::t C;
+    int fi = -1, li = 0, np = 0;
+    for (int i = 0; i < kRadices; i++) {
+        const int c = pass_count(packed, i);
+        if (c) {
+            if (fi < 0) fi = i;
+            li = i;
+            np += c;
+        }
+    }
+    const uint4 pc0 = __ldg(&pc[0]);
+    if (np == 1) {
+#define JV_ONE(R) pass_first<T, R, EMAX, true>(s, ld, nt, pc0, io)
+        JV_RADIX_SWITCH(fi, JV_ONE)
+#undef JV_ONE
+        return;
+    }
+    int Rf = 2;
+#define JV_FIRST(R) (pass_first<T, R, EMAX, false>(s, ld, nt, pc0, io), Rf = R)
+    JV_RADIX_SWITCH(fi, JV_FIRST)
+#undef JV_FIRST
+    int Ns = Rf, p = 1;
+    const C *tp = twg + Rf;
+    const unsigned long long mid = packed - (1ull << (4 * fi)) - (1ull << (4 * li));
+    smem_passes_from<T, EMAX>(s, ld, nt, mid, tp, pc, Ns, p);
+    const uint4 pcl = __ldg(&pc[p]);
+#define JV_LAST(R) pass_last<T, R, EMAX>(s, ld, nt, Ns, tp, pcl, io)
+    JV_RADIX_SWITCH(li, JV_LAST)
+#undef JV_LAST
+}
+
+// smem_passes starting from pass p with Ns and the table pointer tp (updated)
+template <typename T, int EMAX>
+__device__ __forceinline__ void smem_passes_from(typename cplx_t<T>::t *s, int ld, int nt, unsigned long long packed,
+                                                 const typename cplx_t<T>::t *__restrict__ &tp,
+                                                 const uint4 *__restrict__ pc, int &Ns, int &p) {
+#define JV_PASS_LOOP(I, R)                                                  \
+    for (int q = pass_count(packed, I); q > 0; q--, p++) {                  \
+        smem_pass<T, R, EMAX>(s, ld, nt, Ns, tp, __ldg(&pc[p]));            \
+        tp += R * Ns;                                                       \
+        Ns *= R;                                                            \
+    }
+    JV_PASS_LOOP(0, 16)
+    JV_PASS_LOOP(1, 15)
+    JV_PASS_LOOP(2, 14)
+    JV_PASS_LOOP(3, 12)
+    JV_PASS_LOOP(4, 10)
+    JV_PASS_LOOP(5, 9)
+    JV_PASS_LOOP(6, 8)
+    JV_PASS_LOOP(7, 7)
+    JV_PASS_LOOP(8, 6)
+    JV_PASS_LOOP(9, 5)
+    JV_PASS_LOOP(10, 4)
+    JV_PASS_LOOP(11, 3)
+    JV_PASS_LOOP(12, 2)
+#undef JV_PASS_LOOP
 }
 
 // Walker over element (t, n) of a tile (t < nt transforms, n < L elements) of
 // a view with vector stride vs and element stride es, from global index g0
 // (transform v0, element 0).  vf: consecutive threads take consecutive
 // transforms (a = n, b = t), else consecutive elements (a = t, b = n).
-__device__ __forceinline__ void walk_tile(Walk &w, bool vf, int nt, int L, long vs, long es, long g0) {
-    if (vf) w.init(threadIdx.x, blockDim.x, nt, es, vs, g0);
-    else w.init(threadIdx.x, blockDim.x, L, vs, es, g0);
+// exact: the launch-time constants c describe this tile (always for row
+// tiles; for column tiles unless this is a shorter last tile).
+__device__ __forceinline__ void walk_tile(Walk &w, bool vf, int nt, int L, long vs, long es, long g0,
+                                          const WalkConst c, bool exact) {
+    if (exact) {
+        if (vf) w.init_c(c, es, vs, g0);
+        else w.init_c(c, vs, es, g0);
+    } else if (vf) {
+        w.init(threadIdx.x, blockDim.x, nt, es, vs, g0);
+    } else {
+        w.init(threadIdx.x, blockDim.x, L, vs, es, g0);
+    }
 }
 
 // Copies tot tile elements from global to shared memory (row pitch ld, padded
@@ -403,7 +744,7 @@ __device__ __forceinline__ void tile_load(Walk &w, bool vf, int tot, C *s, int l
     }
 }
 
-template <typename T, int EMAX, int MAXT>
+template <typename T, int KIND, int EMAX, int MAXT>
 __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
     typedef typename cplx_t<T>::t C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -424,21 +765,38 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
         if (g >= ngroups) return;
         const long v0 = g * a.vpb;
         const int nt = (int)min((long)a.vpb, a.nvec - v0);
+        if (KIND == K_C2C && a.passes != 0) {
+            // c2c: first pass from the view, last pass to the view
+            TileIO<T> io;
+            io.in = cin;
+            io.out = cout;
+            io.gin = cin.off + v0 * cin.vs;
+            io.gout = cout.off + v0 * cout.vs;
+            io.vf = a.vec_fast != 0;
+            io.conj = a.inv != 0;
+            io.has_scale = a.has_scale != 0;
+            io.scale = a.scale;
+            io.mnt = (nt == a.vpb) ? a.mvpb : magic_of((unsigned)nt);
+            c2c_tile<T, EMAX>(s, ld, nt, a.passes, a.twg, a.pc, io);
+            return;
+        }
         // ---------------- load phase
         const bool vf = a.vec_fast != 0;
+        const bool exact = !vf || nt == a.vpb;
+        const WalkConst win = a.win, wout = a.wout;
         constexpr int LB = (sizeof(T) == 4 && EMAX <= 8) ? 8 : 4;  // loads in flight per thread
         Walk w;
-        if (a.kind == K_C2C) {
-            walk_tile(w, vf, nt, N, cin.vs, cin.es, cin.off + v0 * cin.vs);
+        if (KIND == K_C2C) {
+            walk_tile(w, vf, nt, N, cin.vs, cin.es, cin.off + v0 * cin.vs, win, exact);
             tile_load<LB>(w, vf, nt * N, s, ld, a.inv != 0, [&](long g) { return cin.at(g); });
-        } else if (a.kind == K_R2C) {
+        } else if (KIND == K_R2C) {
             // z_n = x_{2n} + i x_{2n+1}  (c_VSIP_src/VI_rcfftmop_f_def.h:53-75)
-            walk_tile(w, vf, nt, N, rin.vs, 2 * rin.es, rin.off + v0 * rin.vs);
+            walk_tile(w, vf, nt, N, rin.vs, 2 * rin.es, rin.off + v0 * rin.vs, win, exact);
             tile_load<LB>(w, vf, nt * N, s, ld, false,
                           [&](long g) { return mk<C>(rin.a[rin.rst * g], rin.a[rin.rst * (g + rin.es)]); });
         } else {
             // C2R: raw Z_k, k <= N, then the inverse split (VI_crfftmop_f_def.h:58-110)
-            walk_tile(w, vf, nt, N + 1, cin.vs, cin.es, cin.off + v0 * cin.vs);
+            walk_tile(w, vf, nt, N + 1, cin.vs, cin.es, cin.off + v0 * cin.vs, win, exact);
             tile_load<LB>(w, vf, nt * (N + 1), s, ld, false, [&](long g) { return cin.at(g); });
             __syncthreads();
             const int half = N / 2 + 1;   // pairs (k, N-k), k = 0..N/2
@@ -466,11 +824,11 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
         }
         __syncthreads();
         // ---------------- radix passes
-        smem_passes<T, EMAX>(s, ld, N, nt, a.n8, a.n4, a.n2, a.n3, a.n5, a.n7, a.twg);
+        smem_passes<T, EMAX>(s, ld, nt, a.passes, a.twg, a.pc);
         // ---------------- store phase
-        if (a.kind == K_C2C) {
+        if (KIND == K_C2C) {
             const int tot = nt * N;
-            walk_tile(w, vf, nt, N, cout.vs, cout.es, cout.off + v0 * cout.vs);
+            walk_tile(w, vf, nt, N, cout.vs, cout.es, cout.off + v0 * cout.vs, wout, exact);
             for (int i = tid; i < tot; i += nthr, w.next()) {
                 const int t = vf ? w.b : w.a, n = vf ? w.a : w.b;
                 C c = s[t * ld + spad(n)];
@@ -478,10 +836,10 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
                 if (a.has_scale) c = cscale(c, a.scale);
                 cout.put(w.g, c);
             }
-        } else if (a.kind == K_R2C) {
+        } else if (KIND == K_R2C) {
             // Hermitian split (VI_rcfftmop_f_def.h:79-118): X_k from Z_k and Z_{N-k} (Z_N = Z_0)
             const int tot = nt * (N + 1);
-            walk_tile(w, vf, nt, N + 1, cout.vs, cout.es, cout.off + v0 * cout.vs);
+            walk_tile(w, vf, nt, N + 1, cout.vs, cout.es, cout.off + v0 * cout.vs, wout, exact);
             for (int i = tid; i < tot; i += nthr, w.next()) {
                 const int t = vf ? w.b : w.a, k = vf ? w.a : w.b;
                 const C *row = s + t * ld;
@@ -499,7 +857,7 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
         } else {
             // x_{2n} = Re y_n, x_{2n+1} = Im y_n (VI_crfftmop_f_def.h:121-124)
             const int tot = nt * N;
-            walk_tile(w, vf, nt, N, rout.vs, 2 * rout.es, rout.off + v0 * rout.vs);
+            walk_tile(w, vf, nt, N, rout.vs, 2 * rout.es, rout.off + v0 * rout.vs, wout, exact);
             for (int i = tid; i < tot; i += nthr, w.next()) {
                 const int t = vf ? w.b : w.a, n = vf ? w.a : w.b;
                 C c = s[t * ld + spad(n)];
@@ -603,7 +961,13 @@ __global__ void __launch_bounds__(256) k_gpass(const GPassArgs<T> pa) {
             case 4: gpass_body<T, 4>(a, v, j); break;
             case 5: gpass_body<T, 5>(a, v, j); break;
             case 7: gpass_body<T, 7>(a, v, j); break;
+            case 6: gpass_body<T, 6>(a, v, j); break;
             case 8: gpass_body<T, 8>(a, v, j); break;
+            case 9: gpass_body<T, 9>(a, v, j); break;
+            case 10: gpass_body<T, 10>(a, v, j); break;
+            case 12: gpass_body<T, 12>(a, v, j); break;
+            case 14: gpass_body<T, 14>(a, v, j); break;
+            case 15: gpass_body<T, 15>(a, v, j); break;
             case 16: gpass_body<T, 16>(a, v, j); break;
             default: gpass_generic<T>(a, v, j); break;
         }

@@ -79,21 +79,42 @@ long smem_len_limit(int kind) {
     return lim;
 }
 
-// Threads needed so that every pass fits: a thread holds ceil(EMAX/R)
+// Pass counts per codelet (order of kRadixList) packed 4 bits each; false if
+// a radix is not a codelet or a count does not fit.
+inline bool pack_passes(const int *radix, int n, unsigned long long *out) {
+    int cnt[kRadices] = {0};
+    for (int i = 0; i < n; i++) {
+        int r = 0;
+        while (r < kRadices && kRadixList[r] != radix[i]) r++;
+        if (r == kRadices || ++cnt[r] > 15) return false;
+    }
+    // the plan lists its radices in the kernels' loop order (largest first)
+    for (int i = 1; i < n; i++)
+        if (radix[i] > radix[i - 1]) return false;
+    unsigned long long v = 0;
+    for (int r = 0; r < kRadices; r++) v |= (unsigned long long)cnt[r] << (4 * r);
+    *out = v;
+    return true;
+}
+inline bool pack_passes(const std::vector<int> &radix, unsigned long long *out) {
+    return pack_passes(radix.data(), (int)radix.size(), out);
+}
+
+// Threads needed so that every pass fits: a thread holds pass_k(EMAX, R)
 // butterflies of radix R.
 template <int EMAX>
 static long threads_needed(const Job &j, long elems) {
     long need = 32;
     for (int i = 0; i < j.npass; i++) {
         long R = j.radix[i];
-        long K = (EMAX + R - 1) / R;
+        long K = pass_k(EMAX, (int)R);
         long t = (elems / R + K - 1) / K;
         if (t > need) need = t;
     }
     return ((need + 31) / 32) * 32;
 }
 
-template <typename T, int EMAX, int MAXT>
+template <typename T, int KIND, int EMAX, int MAXT>
 static bool launch_smem_v(SmemArgs<T> &a, const Job &j, long vpb, long ld, cudaStream_t st) {
     typedef typename cplx_t<T>::t C;
     Device *d = device();
@@ -104,11 +125,17 @@ static bool launch_smem_v(SmemArgs<T> &a, const Job &j, long vpb, long ld, cudaS
         return false;
     }
     a.vpb = (int)vpb;
+    a.mvpb = magic_host((unsigned long)vpb);
     a.ld = (int)ld;
+    {
+        const long Lin = j.N + (j.kind == K_C2R ? 1 : 0), Lout = j.N + (j.kind == K_R2C ? 1 : 0);
+        a.win = walk_const(a.vec_fast ? vpb : Lin, nthr);
+        a.wout = walk_const(a.vec_fast ? vpb : Lout, nthr);
+    }
     size_t smem = (size_t)vpb * ld * sizeof(C);
     static bool attr_set = false;
     if (!attr_set) {
-        if (!cuda_ok(cudaFuncSetAttribute(k_smem<T, EMAX, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        if (!cuda_ok(cudaFuncSetAttribute(k_smem<T, KIND, EMAX, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)d->smem_optin),
                      "cudaFuncSetAttribute"))
             return false;
@@ -119,12 +146,14 @@ static bool launch_smem_v(SmemArgs<T> &a, const Job &j, long vpb, long ld, cudaS
         set_error(E_UNSUPPORTED, "too many transforms for one launch");
         return false;
     }
-    k_smem<T, EMAX, MAXT><<<(unsigned)grid, (unsigned)nthr, smem, st>>>(a);
+    k_smem<T, KIND, EMAX, MAXT><<<(unsigned)grid, (unsigned)nthr, smem, st>>>(a);
     count_launch();
     return cuda_ok(cudaGetLastError(), "k_smem launch");
 }
 
-template <typename T>
+// The shared-memory kernel for transform kind KIND (one instantiation per
+// kind keeps each kind's register allocation to its own code).
+template <typename T, int KIND>
 bool launch_smem_t(const Job &j, cudaStream_t st) {
     typedef typename cplx_t<T>::t C;
     typedef KCfg<T> K;
@@ -139,18 +168,11 @@ bool launch_smem_t(const Job &j, cudaStream_t st) {
     a.inv = j.inv;
     a.has_scale = j.has_scale;
     a.scale = (T)j.scale;
-    // the plan lists its radices in the kernel's order: 8s, 4, 2, 3s, 5s, 7s
-    for (int i = 0; i < j.npass; i++) {
-        switch (j.radix[i]) {
-            case 8: a.n8++; break;
-            case 4: a.n4++; break;
-            case 2: a.n2++; break;
-            case 3: a.n3++; break;
-            case 5: a.n5++; break;
-            case 7: a.n7++; break;
-            default: set_error(E_UNSUPPORTED, "radix not handled by the shared-memory kernel"); return false;
-        }
+    if (!pack_passes(j.radix, j.npass, &a.passes) || !j.pc) {
+        set_error(E_UNSUPPORTED, "pass schedule not handled by the shared-memory kernel");
+        return false;
     }
+    a.pc = (const uint4 *)j.pc;
     a.cin = cacc<T>(j.cin);
     a.cout = csto<T>(j.cout);
     a.rin = racc<T>(j.rin);
@@ -190,15 +212,17 @@ bool launch_smem_t(const Job &j, cudaStream_t st) {
         if (vpb < 1) vpb = 1;
     }
     size_t cap = d->smem_optin;
-    while (vpb > 1 && ((size_t)vpb * ld * sizeof(C) > cap || vpb * N > elem_cap)) vpb--;
+    while (vpb > 1 && ((size_t)vpb * ld * sizeof(C) > cap || vpb * N > elem_cap ||
+                       threads_needed<K::EMAX_L>(j, vpb * N) > K::MAXT_L))
+        vpb--;
     if (vpb > j.nvec) vpb = j.nvec;
     if ((size_t)vpb * ld * sizeof(C) > cap || vpb * N > elem_cap) {
         set_error(E_UNSUPPORTED, "length too large for the shared-memory kernel");
         return false;
     }
     if (threads_needed<K::EMAX_S>(j, vpb * N) <= K::MAXT_S)
-        return launch_smem_v<T, K::EMAX_S, K::MAXT_S>(a, j, vpb, ld, st);
-    return launch_smem_v<T, K::EMAX_L, K::MAXT_L>(a, j, vpb, ld, st);
+        return launch_smem_v<T, KIND, K::EMAX_S, K::MAXT_S>(a, j, vpb, ld, st);
+    return launch_smem_v<T, KIND, K::EMAX_L, K::MAXT_L>(a, j, vpb, ld, st);
 }
 
 template <typename T>

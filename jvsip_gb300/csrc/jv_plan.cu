@@ -12,6 +12,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <new>
@@ -63,10 +65,76 @@ static unsigned long ref_jofk(unsigned long k, const unsigned long *pn, const un
     return pF * j + (m - s * pF);
 }
 
-std::vector<int> pass_radices(long N, bool *smooth) {
+// Exponents of 2, 3, 5, 7 in each radix of kRadixList (same order).
+static const int kRadE[kRadices][4] = {{4, 0, 0, 0}, {0, 1, 1, 0}, {1, 0, 0, 1}, {2, 1, 0, 0}, {1, 0, 1, 0},
+                                 {0, 2, 0, 0}, {3, 0, 0, 0}, {0, 0, 0, 1}, {1, 1, 0, 0}, {0, 0, 1, 0},
+                                 {2, 0, 0, 0}, {0, 1, 0, 0}, {1, 0, 0, 0}};
+
+// Fewest passes for 2^a 3^b 5^c 7^d using radices whose R * pass_k(16, R)
+// (points a thread holds in that pass with 16-point registers) is at least
+// `need`; ties go to the schedule with the larger radices first.  Returns
+// false when no schedule exists.
+static bool best_schedule(int a, int b, int c, int d, long need, std::vector<int> &out,
+                          std::map<std::tuple<int, int, int, int>, std::vector<int>> &memo,
+                          std::map<std::tuple<int, int, int, int>, bool> &ok) {
+    auto key = std::make_tuple(a, b, c, d);
+    auto it = ok.find(key);
+    if (it != ok.end()) {
+        if (it->second) out = memo[key];
+        return it->second;
+    }
+    if (a == 0 && b == 0 && c == 0 && d == 0) {
+        out.clear();
+        ok[key] = true;
+        memo[key] = out;
+        return true;
+    }
+    bool found = false;
+    std::vector<int> best;
+    for (int i = 0; i < kRadices; i++) {
+        const int R = kRadixList[i];
+        const long K = pass_k(16, R);
+        if ((long)R * K < need) continue;
+        const int *e = kRadE[i];
+        if (e[0] > a || e[1] > b || e[2] > c || e[3] > d) continue;
+        std::vector<int> sub;
+        if (!best_schedule(a - e[0], b - e[1], c - e[2], d - e[3], need, sub, memo, ok)) continue;
+        sub.push_back(R);
+        std::sort(sub.begin(), sub.end(), std::greater<int>());
+        if (!found || sub.size() < best.size() || (sub.size() == best.size() && sub > best)) {
+            best = sub;
+            found = true;
+        }
+    }
+    ok[key] = found;
+    if (found) memo[key] = best;
+    out = best;
+    return found;
+}
+
+std::vector<int> pass_radices(long N, bool *smooth, long maxt) {
     std::vector<int> r;
     *smooth = true;
     if (N <= 1) return r;
+    {
+        // 2^a 3^b 5^c 7^d: the searched schedule (every pass fits maxt threads
+        // for one transform of N points)
+        long n = N;
+        int ex[4] = {0, 0, 0, 0};
+        const int pr[4] = {2, 3, 5, 7};
+        for (int i = 0; i < 4; i++)
+            while (n % pr[i] == 0) {
+                n /= pr[i];
+                ex[i]++;
+            }
+        if (n == 1) {
+            std::map<std::tuple<int, int, int, int>, std::vector<int>> memo;
+            std::map<std::tuple<int, int, int, int>, bool> ok;
+            const long need = (N + maxt - 1) / maxt;
+            if (best_schedule(ex[0], ex[1], ex[2], ex[3], need, r, memo, ok)) return r;
+            r.clear();
+        }
+    }
     long n = N;
     int twos = 0;
     while (n % 2 == 0) {
@@ -117,7 +185,7 @@ static void unit_root(long m, long N, double *c, double *s) {
 // Device tables are shared by all plans of one (length, precision, kind):
 // a batch of thousands of plans over a few hundred lengths keeps one copy.
 struct TableSet {
-    void *tw = nullptr, *thalf = nullptr, *twp = nullptr, *twg = nullptr;
+    void *tw = nullptr, *thalf = nullptr, *twp = nullptr, *twg = nullptr, *pc = nullptr;
     int refs = 0;
 };
 static std::mutex g_tab_mu;
@@ -139,6 +207,7 @@ static bool make_tables(Plan *p) {
         p->d_thalf = it->second.thalf;
         p->d_twp = it->second.twp;
         p->d_twg = it->second.twg;
+        p->d_pc = it->second.pc;
         return true;
     }
     if (!build_tables<T>(p)) return false;
@@ -147,6 +216,7 @@ static bool make_tables(Plan *p) {
     ts.thalf = p->d_thalf;
     ts.twp = p->d_twp;
     ts.twg = p->d_twg;
+    ts.pc = p->d_pc;
     ts.refs = 1;
     g_tabs[key] = ts;
     return true;
@@ -164,6 +234,7 @@ static void release_tables(Plan *p) {
     dfree(p->d_thalf);
     dfree(p->d_twp);
     dfree(p->d_twg);
+    dfree(p->d_pc);
 }
 
 template <typename T>
@@ -205,6 +276,23 @@ static bool build_tables(Plan *p) {
                        "pass twiddle upload");
     };
     if (p->smooth && !pass_tables(p->radix, &p->d_twg)) return false;
+    if (p->smooth) {
+        std::vector<PassConst> pc(std::max<size_t>(1, p->radix.size()));
+        unsigned long Ns = 1;
+        for (size_t i = 0; i < p->radix.size(); i++) {
+            const unsigned long NR = (unsigned long)MN / (unsigned long)p->radix[i];
+            pc[i].NR = (unsigned)NR;
+            pc[i].mNR = magic_host(NR);
+            pc[i].Ns = (unsigned)Ns;
+            pc[i].mNs = magic_host(Ns);
+            Ns *= (unsigned long)p->radix[i];
+        }
+        p->d_pc = dmalloc(pc.size() * sizeof(PassConst));
+        if (!p->d_pc) return false;
+        if (!cuda_ok(cudaMemcpy(p->d_pc, pc.data(), pc.size() * sizeof(PassConst), cudaMemcpyHostToDevice),
+                     "pass constants upload"))
+            return false;
+    }
     if (sizeof(T) == 4) {
         std::vector<int> fr = fast_radices(MN);
         if (!fr.empty() && !pass_tables(fr, &p->d_twp)) return false;
@@ -275,7 +363,7 @@ static VP *create(int type, vsip_length M, vsip_length N, double scale, int dir,
     p->scale = scale;
     p->ntimes = ntimes;
     p->hint = (int)hint;
-    p->radix = pass_radices(p->MN, &p->smooth);
+    p->radix = pass_radices(p->MN, &p->smooth, p->prec == P_F32 ? 1024 : 512);
     unsigned long pn[8], p0[8], pF[8];
     unsigned long ns = ref_factor((unsigned long)p->MN, pn, p0, pF);
     if (ns > 0) {
@@ -287,6 +375,7 @@ static VP *create(int type, vsip_length M, vsip_length N, double scale, int dir,
         dfree(p->d_thalf);
         dfree(p->d_twp);
         dfree(p->d_twg);
+        dfree(p->d_pc);
         delete p;
         free(vp);
         return NULL;
