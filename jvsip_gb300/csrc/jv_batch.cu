@@ -45,26 +45,15 @@ constexpr int BEMAX = 16;     // complex values a thread keeps per pass: tiles o
 
 __device__ __forceinline__ void batch_tile(const TileDesc &d, float2 *s) {
     TileIO<float> io;
-    io.in.re = d.in;
-    io.in.im = d.in + 1;
-    io.in.cst = 2;
-    io.in.off = d.in_off;
-    io.in.es = d.in_es;
-    io.in.vs = d.in_vs;
-    io.in.vec = true;
-    io.out.re = d.out;
-    io.out.im = d.out + 1;
-    io.out.cst = 2;
-    io.out.off = d.out_off;
-    io.out.es = d.out_es;
-    io.out.vs = d.out_vs;
-    io.out.vec = true;
-    io.gin = d.in_off + d.v0 * d.in_vs;
-    io.gout = d.out_off + d.v0 * d.out_vs;
+    io.in = reinterpret_cast<const float2 *>(d.in) + (d.in_off + d.v0 * d.in_vs);
+    io.out = reinterpret_cast<float2 *>(d.out) + (d.out_off + d.v0 * d.out_vs);
+    io.in_es = d.in_es;
+    io.in_vs = d.in_vs;
+    io.out_es = d.out_es;
+    io.out_vs = d.out_vs;
+    io.sgn = d.inv ? -1.f : 1.f;
+    io.scale = d.has_scale ? d.scale : 1.f;
     io.vf = d.vec_fast != 0;
-    io.conj = d.inv != 0;
-    io.has_scale = d.has_scale != 0;
-    io.scale = d.scale;
     io.mnt = d.mnt;
     c2c_tile<float, BEMAX>(s, d.ld, d.nt, d.passes, d.twg, d.pc, io);
 }

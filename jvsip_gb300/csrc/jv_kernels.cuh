@@ -501,13 +501,13 @@ __device__ __forceinline__ void smem_passes(typename cplx_t<T>::t *s, int ld, in
 // j fastest for row tiles (consecutive threads read consecutive elements),
 // t fastest for column tiles (consecutive threads read adjacent transforms).
 template <typename T> struct TileIO {
-    CAcc<T> in;
-    CSto<T> out;
-    long gin, gout;  // global index of element 0 of the tile's first transform
+    typedef typename cplx_t<T>::t C;
+    const C *in;     // interleaved input; element (t, n) at in[t*in_vs + n*in_es]
+    C *out;          // interleaved output; element (t, n) at out[t*out_vs + n*out_es]
+    long in_es, in_vs, out_es, out_vs;
+    T sgn;           // -1: inverse (conjugate on load and on store), else +1
+    T scale;         // 1 when the plan has no scale (x * 1 is exact)
     bool vf;         // t-fastest mapping
-    bool conj;       // inverse: conjugate on load and on store
-    bool has_scale;
-    T scale;
     unsigned mnt;    // multiply-high magic of the tile's transform count
 };
 
@@ -537,11 +537,12 @@ __device__ __forceinline__ void pass_first(typename cplx_t<T>::t *s, int ld, int
         if (b < nb) {
             int t, j;
             tile_tj(b, io.vf, nt, io.mnt, NR, pc.y, t, j);
-            const long g = io.gin + (long)t * io.in.vs + (long)j * io.in.es, st = (long)NR * io.in.es;
+            const C *src = io.in + ((long)t * io.in_vs + (long)j * io.in_es);
+            const long st = (long)NR * io.in_es;
 #pragma unroll
             for (int r = 0; r < R; r++) {
-                C c = io.in.at(g + r * st);
-                if (io.conj) c.y = -c.y;
+                C c = src[r * st];
+                c.y *= io.sgn;
                 v[k][r] = c;
             }
         }
@@ -555,14 +556,10 @@ __device__ __forceinline__ void pass_first(typename cplx_t<T>::t *s, int ld, int
             Dft<C, R>::run(v[k]);
             if (LAST) {
                 // one pass: N = R, j = 0, output element r
-                const long g = io.gout + (long)t * io.out.vs;
+                C *dst = io.out + (long)t * io.out_vs;
+                const T sy = io.sgn * io.scale;
 #pragma unroll
-                for (int r = 0; r < R; r++) {
-                    C c = v[k][r];
-                    if (io.conj) c.y = -c.y;
-                    if (io.has_scale) c = cscale(c, io.scale);
-                    io.out.put(g + (long)r * io.out.es, c);
-                }
+                for (int r = 0; r < R; r++) dst[r * io.out_es] = mk<C>(v[k][r].x * io.scale, v[k][r].y * sy);
             } else {
                 C *dst = s + t * ld;
 #pragma unroll
@@ -594,6 +591,7 @@ __device__ __forceinline__ void pass_last(const typename cplx_t<T>::t *s, int ld
             for (int r = 0; r < R; r++) v[k][r] = src[spad(j + r * NR)];
         }
     }
+    const T sy = io.sgn * io.scale;
 #pragma unroll
     for (int k = 0; k < K; k++) {
         const int b = tid + k * nthr;
@@ -605,14 +603,10 @@ __device__ __forceinline__ void pass_last(const typename cplx_t<T>::t *s, int ld
                 for (int r = 1; r < R; r++) v[k][r] = cmul(v[k][r], __ldg(&tp[r * Ns + j]));
             }
             Dft<C, R>::run(v[k]);
-            const long g = io.gout + (long)t * io.out.vs + (long)j * io.out.es, st = (long)Ns * io.out.es;
+            C *dst = io.out + ((long)t * io.out_vs + (long)j * io.out_es);
+            const long st = (long)Ns * io.out_es;
 #pragma unroll
-            for (int r = 0; r < R; r++) {
-                C c = v[k][r];
-                if (io.conj) c.y = -c.y;
-                if (io.has_scale) c = cscale(c, io.scale);
-                io.out.put(g + r * st, c);
-            }
+            for (int r = 0; r < R; r++) dst[r * st] = mk<C>(v[k][r].x * io.scale, v[k][r].y * sy);
         }
     }
 }
@@ -765,17 +759,18 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
         if (g >= ngroups) return;
         const long v0 = g * a.vpb;
         const int nt = (int)min((long)a.vpb, a.nvec - v0);
-        if (KIND == K_C2C && a.passes != 0) {
-            // c2c: first pass from the view, last pass to the view
+        if (KIND == K_C2C && a.passes != 0 && cin.vec && cout.vec) {
+            // c2c on interleaved views: first pass from the view, last pass to the view
             TileIO<T> io;
-            io.in = cin;
-            io.out = cout;
-            io.gin = cin.off + v0 * cin.vs;
-            io.gout = cout.off + v0 * cout.vs;
+            io.in = reinterpret_cast<const C *>(cin.re) + (cin.off + v0 * cin.vs);
+            io.out = reinterpret_cast<C *>(cout.re) + (cout.off + v0 * cout.vs);
+            io.in_es = cin.es;
+            io.in_vs = cin.vs;
+            io.out_es = cout.es;
+            io.out_vs = cout.vs;
+            io.sgn = a.inv ? (T)-1 : (T)1;
+            io.scale = a.has_scale ? a.scale : (T)1;
             io.vf = a.vec_fast != 0;
-            io.conj = a.inv != 0;
-            io.has_scale = a.has_scale != 0;
-            io.scale = a.scale;
             io.mnt = (nt == a.vpb) ? a.mvpb : magic_of((unsigned)nt);
             c2c_tile<T, EMAX>(s, ld, nt, a.passes, a.twg, a.pc, io);
             return;
