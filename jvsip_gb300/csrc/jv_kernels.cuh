@@ -410,6 +410,7 @@ template <typename T> struct SmemArgs {
     unsigned long long passes;  // pass counts per codelet (pass_count)
     const uint4 *pc;  // per-pass constants of the schedule (NR, magic NR, Ns, magic Ns)
     unsigned mvpb;    // multiply-high magic of vpb
+    int real_pairs;   // R2C input / C2R output rows: unit stride, even offset and pitch, 2-element aligned
     WalkConst win, wout;  // load / store walker constants for full tiles of vpb transforms
     CAcc<T> cin;
     CSto<T> cout;
@@ -628,12 +629,13 @@ __device__ __forceinline__ void pass_last(const typename cplx_t<T>::t *s, int ld
         default: CALL(2); break; \
     }
 
-// A whole c2c tile: global -> passes -> global.  The schedule must have at
-// least one pass.
-template <typename T, int EMAX>
-__device__ __forceinline__ void c2c_tile(typename cplx_t<T>::t *s, int ld, int nt, unsigned long long packed,
-                                         const typename cplx_t<T>::t *__restrict__ twg,
-                                         const uint4 *__restrict__ pc, const TileIO<T> &io) {
+// The passes of a tile with the first pass reading the view (FROMG) and/or the
+// last pass writing the view (TOG) through io; otherwise those passes run in
+// shared memory like the middle ones.  The schedule must have at least one pass.
+template <typename T, int EMAX, bool FROMG, bool TOG>
+__device__ __forceinline__ void tile_passes(typename cplx_t<T>::t *s, int ld, int nt, unsigned long long packed,
+                                            const typename cplx_t<T>::t *__restrict__ twg,
+                                            const uint4 *__restrict__ pc, const TileIO<T> &io) {
     typedef typename cplx_t<T>::t C;
     int fi = -1, li = 0, np = 0;
     for (int i = 0; i < kRadices; i++) {
@@ -644,25 +646,42 @@ __device__ __forceinline__ void c2c_tile(typename cplx_t<T>::t *s, int ld, int n
             np += c;
         }
     }
-    const uint4 pc0 = __ldg(&pc[0]);
-    if (np == 1) {
+    int Ns = 1, p = 0;
+    const C *tp = twg;
+    unsigned long long mid = packed;
+    if (FROMG) {
+        const uint4 pc0 = __ldg(&pc[0]);
+        if (TOG && np == 1) {
 #define JV_ONE(R) pass_first<T, R, EMAX, true>(s, ld, nt, pc0, io)
-        JV_RADIX_SWITCH(fi, JV_ONE)
+            JV_RADIX_SWITCH(fi, JV_ONE)
 #undef JV_ONE
-        return;
-    }
-    int Rf = 2;
+            return;
+        }
+        int Rf = 2;
 #define JV_FIRST(R) (pass_first<T, R, EMAX, false>(s, ld, nt, pc0, io), Rf = R)
-    JV_RADIX_SWITCH(fi, JV_FIRST)
+        JV_RADIX_SWITCH(fi, JV_FIRST)
 #undef JV_FIRST
-    int Ns = Rf, p = 1;
-    const C *tp = twg + Rf;
-    const unsigned long long mid = packed - (1ull << (4 * fi)) - (1ull << (4 * li));
+        Ns = Rf;
+        p = 1;
+        tp += Rf;
+        mid -= 1ull << (4 * fi);
+        np--;
+    }
+    if (TOG && np > 0) mid -= 1ull << (4 * li);
     smem_passes_from<T, EMAX>(s, ld, nt, mid, tp, pc, Ns, p);
-    const uint4 pcl = __ldg(&pc[p]);
+    if (TOG && np > 0) {
+        const uint4 pcl = __ldg(&pc[p]);
 #define JV_LAST(R) pass_last<T, R, EMAX>(s, ld, nt, Ns, tp, pcl, io)
-    JV_RADIX_SWITCH(li, JV_LAST)
+        JV_RADIX_SWITCH(li, JV_LAST)
 #undef JV_LAST
+    }
+}
+
+template <typename T, int EMAX>
+__device__ __forceinline__ void c2c_tile(typename cplx_t<T>::t *s, int ld, int nt, unsigned long long packed,
+                                         const typename cplx_t<T>::t *__restrict__ twg,
+                                         const uint4 *__restrict__ pc, const TileIO<T> &io) {
+    tile_passes<T, EMAX, true, true>(s, ld, nt, packed, twg, pc, io);
 }
 
 // smem_passes starting from pass p with Ns and the table pointer tp (updated)
@@ -780,7 +799,24 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
         const bool exact = !vf || nt == a.vpb;
         const WalkConst win = a.win, wout = a.wout;
         constexpr int LB = (sizeof(T) == 4 && EMAX <= 8) ? 8 : 4;  // loads in flight per thread
+        // real rows of unit stride, even offset and pitch: x_{2n}, x_{2n+1} are
+        // one interleaved complex element, so the R2C first pass reads them
+        // from the view and the C2R last pass writes them to the view
+        const bool rp = (KIND != K_C2C) && a.real_pairs && a.passes != 0;
         Walk w;
+        if (KIND == K_R2C && rp) {
+            TileIO<T> io;
+            io.in = reinterpret_cast<const C *>(rin.a + (rin.off + v0 * rin.vs));
+            io.out = nullptr;
+            io.in_es = 1;
+            io.in_vs = rin.vs / 2;
+            io.out_es = io.out_vs = 0;
+            io.sgn = (T)1;
+            io.scale = (T)1;
+            io.vf = false;
+            io.mnt = 0;
+            tile_passes<T, EMAX, true, false>(s, ld, nt, a.passes, a.twg, a.pc, io);
+        } else {
         if (KIND == K_C2C) {
             walk_tile(w, vf, nt, N, cin.vs, cin.es, cin.off + v0 * cin.vs, win, exact);
             tile_load<LB>(w, vf, nt * N, s, ld, a.inv != 0, [&](long g) { return cin.at(g); });
@@ -818,8 +854,25 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
             }
         }
         __syncthreads();
+        if (KIND == K_C2R && rp) {
+            // x_{2n} = Re y_n, x_{2n+1} = Im y_n (VI_crfftmop_f_def.h:121-124)
+            // written by the last pass: y conjugated back, scaled
+            TileIO<T> io;
+            io.in = nullptr;
+            io.out = reinterpret_cast<C *>(rout.a + (rout.off + v0 * rout.vs));
+            io.in_es = io.in_vs = 0;
+            io.out_es = 1;
+            io.out_vs = rout.vs / 2;
+            io.sgn = (T)-1;
+            io.scale = a.has_scale ? a.scale : (T)1;
+            io.vf = false;
+            io.mnt = 0;
+            tile_passes<T, EMAX, false, true>(s, ld, nt, a.passes, a.twg, a.pc, io);
+            return;
+        }
         // ---------------- radix passes
         smem_passes<T, EMAX>(s, ld, nt, a.passes, a.twg, a.pc);
+        }
         // ---------------- store phase
         if (KIND == K_C2C) {
             const int tot = nt * N;

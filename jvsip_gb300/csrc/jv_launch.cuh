@@ -187,6 +187,13 @@ bool launch_smem_t(const Job &j, cudaStream_t st) {
     bool vf_in = labs_(vs_in) == 1 && labs_(es_in) != 1;
     bool vf_out = labs_(vs_out) == 1 && labs_(es_out) != 1;
     a.vec_fast = (vf_in || vf_out) ? 1 : 0;
+    {
+        const RView &rv = (j.kind == K_R2C) ? j.rin : j.rout;
+        a.real_pairs = (j.kind != K_C2C && !a.vec_fast && rv.rst == 1 && rv.es == 1 && rv.off % 2 == 0 &&
+                        rv.vs % 2 == 0 && rv.vs > 0 && ((uintptr_t)rv.a % (2 * sizeof(T))) == 0)
+                           ? 1
+                           : 0;
+    }
     const long N = j.N;
     // shared-memory rows are indexed i + i/16 (conflict-free Stockham passes)
     const long need = N + (j.kind == K_C2R ? 1 : 0);
