@@ -106,6 +106,8 @@ struct Job {
     int npass = 0;
     int radix[40];
     int form = 0;        // JVSIP_FORM_* of the plan
+    bool no_fast = false;      // JVSIP_GPU_NO_FAST at plan creation: general kernels only
+    bool no_pipeline = false;  // JVSIP_GPU_NO_PIPELINE at plan creation: one staging copy each way
 };
 
 // Kernel entry points (defined in the kernel translation units).
@@ -134,6 +136,8 @@ struct Plan {
     unsigned ntimes = 0;
     int hint = 0;
     int form = 0;             // JVSIP_FORM_*
+    bool no_fast = false;     // environment switches read once at creation
+    bool no_pipeline = false;
     std::vector<int> radix;   // pass radices of the device kernels (product = MN)
     bool smooth = true;       // every radix is one of the built-in codelets
     void *d_tw = nullptr;     // forward twiddles, MN entries

@@ -288,6 +288,8 @@ static void fill_job(Job &j, const Plan *p, int kind) {
     j.twg = p->d_twg;
     j.pc = p->d_pc;
     j.form = p->form;
+    j.no_fast = p->no_fast;
+    j.no_pipeline = p->no_pipeline;
     j.npass = (int)p->radix.size();
     for (int i = 0; i < j.npass && i < 40; i++) j.radix[i] = p->radix[i];
 }
@@ -301,7 +303,7 @@ static void fill_job(Job &j, const Plan *p, int kind) {
 // do not qualify.
 template <typename T, typename CB>
 static bool pipelined_cc(Job &j, const CRes<T, CB> &rx, const CRes<T, CB> &ry, bool same_view, bool *ok) {
-    if (getenv("JVSIP_GPU_NO_PIPELINE")) return false;
+    if (j.no_pipeline) return false;
     if (rx.m || ry.m) return false;
     if (rx.blk->cstride != 2 || ry.blk->cstride != 2) return false;
     const long len = j.N, nv = j.nvec;

@@ -194,7 +194,7 @@ std::vector<int> fast_radices(long N) {
 // Specialised kernels: contiguous interleaved rows, any pitch, forward or
 // inverse (conjugation folded into load and store), optional scale.
 bool launch_fast_f32(const Job &j, cudaStream_t st) {
-    if (getenv("JVSIP_GPU_NO_FAST")) return false;
+    if (j.no_fast) return false;
     if (j.kind != K_C2C || j.prec != P_F32) return false;
     const CView &ci = j.cin, &co = j.cout;
     // interleaved, unit element stride, 8-byte aligned, rows of the transform contiguous

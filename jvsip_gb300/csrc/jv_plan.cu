@@ -361,6 +361,8 @@ static VP *create(int type, vsip_length M, vsip_length N, double scale, int dir,
         p->dir = dir;
     }
     p->scale = scale;
+    p->no_fast = getenv("JVSIP_GPU_NO_FAST") != nullptr;
+    p->no_pipeline = getenv("JVSIP_GPU_NO_PIPELINE") != nullptr;
     p->ntimes = ntimes;
     p->hint = (int)hint;
     p->radix = pass_radices(p->MN, &p->smooth, p->prec == P_F32 ? 1024 : 512);
