@@ -269,7 +269,7 @@ int  jvsip_fftm_batch_destroy_f(jvsip_fftm_batchplan_f *batch);
  * vf = 1 for column transforms) time the batch kernel with each candidate
  * number of FFTs per tile and keep the fastest, in memory and in a versioned
  * cache file keyed by GPU name ($JVSIP_GPU_TUNE_CACHE, default
- * ~/.cache/jvsip_gb300/tune-v1.txt).  Untuned lengths use a heuristic.
+ * ~/.cache/jvsip_gb300/tune-v2.txt).  Untuned lengths use a heuristic.
  * Returns 0 on success; jvsip_fftm_autotune_entries() counts cached keys. */
 int  jvsip_fftm_autotune_f(size_t n, const unsigned long *lengths, int vf);
 long jvsip_fftm_autotune_entries(void);

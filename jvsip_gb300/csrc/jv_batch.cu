@@ -3,11 +3,13 @@
 // majors) in one persistent launch.
 //
 // The host cuts every call into tiles of transforms (FFTs per tile from the
-// autotuner's cache, or the general kernel's heuristic) and uploads one
-// descriptor per tile, largest tiles first.  One launch of 1024-thread CTAs
-// consumes the queue, one descriptor per CTA -- no CTA ever waits on another
-// -- running the general shared-memory passes on each tile.  A captured batch
-// (jvsip_fftm_batch_create_f) records the launch in a CUDA graph once;
+// autotuner's cache, or a heuristic), gives each tile the smallest CTA size
+// (256, 512 or 1024 threads) whose threads cover its passes, and uploads one
+// descriptor queue per size, largest tiles first.  One launch per size
+// consumes its queue, one descriptor per CTA -- no CTA ever waits on another
+// -- running the general kernel's fused c2c passes on each tile; the launches
+// run side by side on forked streams.  A captured batch
+// (jvsip_fftm_batch_create_f) records the launches in a CUDA graph once;
 // jvsip_fftm_batch_run_f replays it.
 //
 // No reference counterpart: VSIPL has no multi-plan call; the reference can
@@ -16,6 +18,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -35,13 +38,18 @@ struct TileDesc {
     unsigned mnt;       // multiply-high magic of nt
     long v0;
     int N, nt, ld;
-    unsigned char inv, vec_fast;
+    unsigned char inv, vec_fast, cls;  // cls: CTA-size class (index into kClassBT)
     int has_scale;
     float scale;
 };
 
-constexpr int BT = 1024;      // threads of a batch CTA
+constexpr int BT = 1024;      // threads of the largest batch CTA
 constexpr int BEMAX = 16;     // complex values a thread keeps per pass: tiles of <= 16384 points
+// CTA-size classes: a tile runs in the smallest CTA whose threads cover every
+// pass of it, so small tiles share an SM (4 x 256 or 2 x 512 threads at 64
+// registers) instead of idling most of a 1024-thread CTA
+constexpr int kClasses = 3;
+constexpr int kClassBT[kClasses] = {256, 512, 1024};
 
 __device__ __forceinline__ void batch_tile(const TileDesc &d, float2 *s) {
     TileIO<float> io;
@@ -65,7 +73,8 @@ __device__ __forceinline__ void batch_tile(const TileDesc &d, float2 *s) {
 // measured against ptxas: keeping the pass state live across tile iterations
 // spills the codelet registers at every block size, so the loop-free form is
 // used.)
-__global__ void __launch_bounds__(BT, 1) k_batch(const TileDesc *__restrict__ q, int ntiles) {
+template <int CBT>
+__global__ void __launch_bounds__(CBT, 1024 / CBT) k_batch(const TileDesc *__restrict__ q, int ntiles) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *s = reinterpret_cast<float2 *>(smem_raw);
     __shared__ TileDesc sd;  // descriptor fields are re-read from shared memory, not held in registers
@@ -78,8 +87,8 @@ __global__ void __launch_bounds__(BT, 1) k_batch(const TileDesc *__restrict__ q,
 
 // ---------------------------------------------------------------- host side
 struct BatchBuild {
-    std::vector<TileDesc> tiles;
-    size_t smem = 0;
+    std::vector<TileDesc> tiles[kClasses];
+    size_t smem[kClasses] = {0, 0, 0};
     double bytes = 0;
 };
 
@@ -185,50 +194,119 @@ static bool build_tiles(size_t n, const vsip_fftm_f *const plans[], const vsip_c
             u.v0 = v0;
             u.nt = (int)std::min(per, nv - v0);
             u.mnt = magic_host((unsigned long)u.nt);
-            bb.tiles.push_back(u);
-            bb.smem = std::max(bb.smem, (size_t)u.nt * u.ld * 8);
+            // threads the tile's passes need: a thread holds pass_k(BEMAX, R) butterflies
+            long need = 32;
+            for (int r : p->radix) {
+                const long K = pass_k(BEMAX, r);
+                need = std::max(need, ((long)u.nt * N / r + K - 1) / K);
+            }
+            int c = 0;
+            while (c < kClasses - 1 && need > kClassBT[c]) c++;
+            u.cls = (unsigned char)c;
+            bb.tiles[c].push_back(u);
+            bb.smem[c] = std::max(bb.smem[c], (size_t)u.nt * u.ld * 8);
         }
         bb.bytes += 16.0 * N * nv;
     }
-    // largest tiles first: the queue's tail is made of short work
-    std::stable_sort(bb.tiles.begin(), bb.tiles.end(), [](const TileDesc &a, const TileDesc &b) {
-        return (long)a.N * a.nt > (long)b.N * b.nt;
-    });
+    // largest tiles first: each queue's tail is made of short work
+    for (int c = 0; c < kClasses; c++)
+        std::stable_sort(bb.tiles[c].begin(), bb.tiles[c].end(), [](const TileDesc &a, const TileDesc &b) {
+            return (long)a.N * a.nt > (long)b.N * b.nt;
+        });
     return true;
 }
 
 struct DevBatch {
-    TileDesc *q = nullptr;
-    int ntiles = 0;
-    size_t smem = 0;
+    TileDesc *q = nullptr;            // the classes' queues, one after the other
+    int off[kClasses] = {0, 0, 0};    // first descriptor of each class
+    int n[kClasses] = {0, 0, 0};      // descriptors of each class
+    size_t smem[kClasses] = {0, 0, 0};
+    int total = 0;
 };
 
 static bool upload(const BatchBuild &bb, DevBatch &db) {
-    db.ntiles = (int)bb.tiles.size();
-    db.smem = bb.smem;
-    db.q = (TileDesc *)dmalloc(std::max<size_t>(1, bb.tiles.size()) * sizeof(TileDesc));
+    std::vector<TileDesc> all;
+    for (int c = 0; c < kClasses; c++) {
+        db.off[c] = (int)all.size();
+        db.n[c] = (int)bb.tiles[c].size();
+        db.smem[c] = bb.smem[c];
+        all.insert(all.end(), bb.tiles[c].begin(), bb.tiles[c].end());
+    }
+    db.total = (int)all.size();
+    db.q = (TileDesc *)dmalloc(std::max<size_t>(1, all.size()) * sizeof(TileDesc));
     if (!db.q) return false;
     Device *d = device();
-    if (!bb.tiles.empty() &&
-        !cuda_ok(cudaMemcpyAsync(db.q, bb.tiles.data(), bb.tiles.size() * sizeof(TileDesc),
-                                 cudaMemcpyHostToDevice, d->stream), "batch queue upload"))
+    if (!all.empty() && !cuda_ok(cudaMemcpyAsync(db.q, all.data(), all.size() * sizeof(TileDesc),
+                                                 cudaMemcpyHostToDevice, d->stream),
+                                 "batch queue upload"))
         return false;
     return true;
 }
 
-static bool launch(const DevBatch &db, cudaStream_t st) {
+template <int CBT>
+static bool launch_class(const DevBatch &db, int c, cudaStream_t st) {
     Device *d = device();
-    if (db.ntiles == 0) return true;
     static bool attr = false;
     if (!attr) {
-        if (!cuda_ok(cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d->smem_optin - 512),
+        if (!cuda_ok(cudaFuncSetAttribute(k_batch<CBT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)d->smem_optin - 512),
                      "cudaFuncSetAttribute"))
             return false;
         attr = true;
     }
-    k_batch<<<db.ntiles, BT, db.smem, st>>>(db.q, db.ntiles);
+    k_batch<CBT><<<db.n[c], CBT, db.smem[c], st>>>(db.q + db.off[c], db.n[c]);
     count_launch();
     return cuda_ok(cudaGetLastError(), "k_batch launch");
+}
+
+static bool launch_one(const DevBatch &db, int c, cudaStream_t st) {
+    switch (c) {
+        case 0: return launch_class<256>(db, c, st);
+        case 1: return launch_class<512>(db, c, st);
+        default: return launch_class<1024>(db, c, st);
+    }
+}
+
+// Streams and events the classes run on side by side (forked from and joined
+// back to the caller's stream; the same pattern is recorded into the graph).
+struct BatchStreams {
+    cudaStream_t s[kClasses] = {nullptr, nullptr, nullptr};
+    cudaEvent_t fork = nullptr, join[kClasses] = {nullptr, nullptr, nullptr};
+    bool ready = false;
+};
+static BatchStreams g_bs;
+static std::mutex g_bs_mu;
+
+static bool batch_streams() {
+    std::lock_guard<std::mutex> lk(g_bs_mu);
+    if (g_bs.ready) return true;
+    bool ok = cuda_ok(cudaEventCreateWithFlags(&g_bs.fork, cudaEventDisableTiming), "batch event");
+    for (int c = 0; c < kClasses && ok; c++)
+        ok = cuda_ok(cudaStreamCreateWithFlags(&g_bs.s[c], cudaStreamNonBlocking), "batch stream") &&
+             cuda_ok(cudaEventCreateWithFlags(&g_bs.join[c], cudaEventDisableTiming), "batch event");
+    g_bs.ready = ok;
+    return ok;
+}
+
+static bool launch(const DevBatch &db, cudaStream_t st) {
+    if (db.total == 0) return true;
+    int used = 0, only = 0;
+    for (int c = 0; c < kClasses; c++)
+        if (db.n[c]) {
+            used++;
+            only = c;
+        }
+    if (used == 1) return launch_one(db, only, st);
+    if (!batch_streams()) return false;
+    bool ok = cuda_ok(cudaEventRecord(g_bs.fork, st), "batch fork");
+    // largest CTAs first: they hold the longest tiles
+    for (int c = kClasses - 1; c >= 0 && ok; c--) {
+        if (!db.n[c]) continue;
+        ok = cuda_ok(cudaStreamWaitEvent(g_bs.s[c], g_bs.fork, 0), "batch fork") && launch_one(db, c, g_bs.s[c]) &&
+             cuda_ok(cudaEventRecord(g_bs.join[c], g_bs.s[c]), "batch join") &&
+             cuda_ok(cudaStreamWaitEvent(st, g_bs.join[c], 0), "batch join");
+    }
+    return ok;
 }
 
 static void free_dev(DevBatch &db) {
@@ -325,7 +403,7 @@ int jvsip_fftm_batch_run_f(jvsip_fftm_batchplan_f *b) {
     if (!b) return E_ARG;
     Device *d = device();
     if (!d) return E_NODEVICE;
-    if (b->db.ntiles == 0) return 0;
+    if (b->db.total == 0) return 0;
     if (!cuda_ok(cudaGraphLaunch(b->exec, d->stream), "batch graph launch")) return E_CUDA;
     count_launch();
     for (const void *blk : b->blocks) {

@@ -5,7 +5,7 @@
 // kernel on scratch data with each candidate number of FFTs per tile (powers
 // of two up to the 16384-point tile limit) and keeps the fastest.  Results
 // live in memory and in a versioned text cache, one line per key, keyed also
-// by the GPU name, in $JVSIP_GPU_TUNE_CACHE or ~/.cache/jvsip_gb300/tune-v1.txt
+// by the GPU name, in $JVSIP_GPU_TUNE_CACHE or ~/.cache/jvsip_gb300/tune-v2.txt
 // (safe to delete).  Lengths that were never tuned use the heuristic below.
 #include <stdio.h>
 #include <stdlib.h>
@@ -30,7 +30,7 @@ static std::string cache_path() {
     const char *e = getenv("JVSIP_GPU_TUNE_CACHE");
     if (e && *e) return e;
     const char *h = getenv("HOME");
-    return std::string(h ? h : "/tmp") + "/.cache/jvsip_gb300/tune-v1.txt";
+    return std::string(h ? h : "/tmp") + "/.cache/jvsip_gb300/tune-v2.txt";
 }
 
 static void load_cache() {
@@ -64,10 +64,11 @@ static void save_entry(long N, int prec, int vf, long per) {
     fclose(f);
 }
 
-// heuristic: about 8192 points per tile for row transforms, 16 columns per
-// tile for column transforms (one 128-byte segment per row of the tile)
+// heuristic: about 4096 points per tile for row transforms (a 256-thread CTA,
+// four per SM), 16 columns per tile for column transforms (one 128-byte
+// segment per row of the tile)
 static long heuristic(long N, bool vf, long rows) {
-    long per = vf ? 16 : std::max(1L, 8192 / N);
+    long per = vf ? 16 : std::max(1L, 4096 / N);
     while (per > 1 && per * N > 16384) per--;
     if (per > rows) per = rows;
     return std::max(1L, per);
