@@ -22,6 +22,8 @@
 #include <new>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "jv_launch.cuh"
 
 namespace jv {
@@ -48,8 +50,9 @@ constexpr int BEMAX = 16;     // complex values a thread keeps per pass: tiles o
 // CTA-size classes: a tile runs in the smallest CTA whose threads cover every
 // pass of it, so small tiles share an SM (4 x 256 or 2 x 512 threads at 64
 // registers) instead of idling most of a 1024-thread CTA
-constexpr int kClasses = 3;
-constexpr int kClassBT[kClasses] = {256, 512, 1024};
+constexpr int kClasses = 4;
+constexpr int kClassBT[kClasses] = {256, 512, 1024, 1024};  // the last: column clusters
+constexpr int kColClass = 3;
 
 __device__ __forceinline__ void batch_tile(const TileDesc &d, float2 *s) {
     TileIO<float> io;
@@ -85,10 +88,98 @@ __global__ void __launch_bounds__(CBT, 1024 / CBT) k_batch(const TileDesc *__res
     batch_tile(sd, s);
 }
 
+// Columns of long transforms (one column fills a CTA): a 4-CTA cluster takes
+// up to 4 adjacent columns, one column per CTA.  CTA c reads rows
+// [c*Q, (c+1)*Q) of all the columns with the column index fastest -- every
+// matrix row is one contiguous segment -- and stores each value into the
+// owning CTA's shared memory (distributed shared memory, natural order); after
+// a cluster barrier every CTA runs its column's passes locally (the first pass
+// reads the natural order, the last writes the padded rows); after a second
+// barrier CTA c writes rows [c*Q, (c+1)*Q) of all the columns, read from the
+// owners' shared memory, and a third barrier keeps every CTA's shared memory
+// alive until the others have read it.  Every thread of the cluster reaches
+// every barrier: CTAs without a column skip only the passes.
+constexpr int kColCluster = 4;
+
+__device__ __forceinline__ void col_passes(float2 *s, int ld, unsigned long long packed, const float2 *twg,
+                                           const uint4 *pc) {
+    int fi = 0;
+    while (fi < kRadices - 1 && pass_count(packed, fi) == 0) fi++;
+    const uint4 pc0 = __ldg(&pc[0]);
+    int Rf = 2;
+#define JV_DENSE_FIRST(R) (smem_pass<float, R, BEMAX, true>(s, ld, 1, 1, twg, pc0), Rf = R)
+    JV_RADIX_SWITCH(fi, JV_DENSE_FIRST)
+#undef JV_DENSE_FIRST
+    int Ns = Rf, p = 1;
+    const float2 *tp = twg + Rf;
+    smem_passes_from<float, BEMAX>(s, ld, 1, packed - (1ull << (4 * fi)), tp, pc, Ns, p);
+}
+
+__global__ void __cluster_dims__(kColCluster, 1, 1) __launch_bounds__(BT, 1)
+    k_batch_cols(const TileDesc *__restrict__ q, int ntiles) {
+    namespace cg = cooperative_groups;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *s = reinterpret_cast<float2 *>(smem_raw);
+    __shared__ TileDesc sd;
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    const int t = blockIdx.x / kColCluster;  // the same descriptor for the whole cluster
+    if (t >= ntiles) return;                 // uniform over the cluster
+    if (threadIdx.x == 0) sd = q[t];
+    __syncthreads();
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int N = sd.N, nt = sd.nt;
+    const int Q = (N + kColCluster - 1) / kColCluster;
+    const int n0 = rank * Q, nr = max(0, min(N, n0 + Q) - n0);
+    const int tot = nr * nt;
+    const unsigned mnt = sd.mnt;
+    const float2 *in = reinterpret_cast<const float2 *>(sd.in) + (sd.in_off + sd.v0 * sd.in_vs);
+    const long ies = sd.in_es, ivs = sd.in_vs;
+    const float sgn = sd.inv ? -1.f : 1.f;
+    // ---- load: (row, column) with the column fastest, four loads in flight
+    for (int i0 = tid; i0 < tot; i0 += 4 * nthr) {
+        float2 c[4];
+        int kk[4], nn[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int i = i0 + u * nthr;
+            kk[u] = 0;
+            nn[u] = 0;
+            if (i < tot) {
+                const int r = mdiv(i, mnt);
+                kk[u] = i - r * nt;
+                nn[u] = n0 + r;
+                c[u] = in[(long)kk[u] * ivs + (long)nn[u] * ies];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            if (i0 + u * nthr < tot) {
+                float2 *dst = cl.map_shared_rank(s, kk[u]);
+                dst[nn[u]] = make_float2(c[u].x, c[u].y * sgn);
+            }
+        }
+    }
+    cl.sync();
+    if (rank < nt) col_passes(s, sd.ld, sd.passes, sd.twg, sd.pc);
+    cl.sync();
+    // ---- store: rows [n0, n0 + nr) of the columns, from their owners
+    float2 *out = reinterpret_cast<float2 *>(sd.out) + (sd.out_off + sd.v0 * sd.out_vs);
+    const long oes = sd.out_es, ovs = sd.out_vs;
+    const float scale = sd.has_scale ? sd.scale : 1.f, sy = sgn * scale;
+    for (int i = tid; i < tot; i += nthr) {
+        const int r = mdiv(i, mnt), k = i - r * nt, n = n0 + r;
+        const float2 *src = cl.map_shared_rank(s, k);
+        const float2 v = src[spad(n)];
+        out[(long)k * ovs + (long)n * oes] = make_float2(v.x * scale, v.y * sy);
+    }
+    cl.sync();
+}
+
 // ---------------------------------------------------------------- host side
 struct BatchBuild {
     std::vector<TileDesc> tiles[kClasses];
-    size_t smem[kClasses] = {0, 0, 0};
+    size_t smem[kClasses] = {0, 0, 0, 0};
     double bytes = 0;
 };
 
@@ -181,6 +272,22 @@ static bool build_tiles(size_t n, const vsip_fftm_f *const plans[], const vsip_c
         bool vf_out = labs(t.out_vs) == 1 && labs(t.out_es) != 1;
         t.vec_fast = (vf_in || vf_out) ? 1 : 0;
         t.ld = (int)tile_ld(N, t.vec_fast);
+        if (t.vec_fast && 2 * N > BEMAX * BT) {
+            // columns of long transforms: groups of up to kColCluster adjacent
+            // columns, one cluster each (k_batch_cols)
+            t.ld = (int)tile_ld(N, false);
+            for (long v0 = 0; v0 < nv; v0 += kColCluster) {
+                TileDesc u = t;
+                u.v0 = v0;
+                u.nt = (int)std::min((long)kColCluster, nv - v0);
+                u.mnt = magic_host((unsigned long)u.nt);
+                u.cls = (unsigned char)kColClass;
+                bb.tiles[kColClass].push_back(u);
+                bb.smem[kColClass] = std::max(bb.smem[kColClass], (size_t)u.ld * 8);
+            }
+            bb.bytes += 16.0 * N * nv;
+            continue;
+        }
         long per = batch_fft_per_tile(N, t.vec_fast, nv);
         // every pass of the tile must fit the CTA: a thread holds
         // pass_k(BEMAX, R) butterflies of radix R (the plan's schedule fits
@@ -218,9 +325,9 @@ static bool build_tiles(size_t n, const vsip_fftm_f *const plans[], const vsip_c
 
 struct DevBatch {
     TileDesc *q = nullptr;            // the classes' queues, one after the other
-    int off[kClasses] = {0, 0, 0};    // first descriptor of each class
-    int n[kClasses] = {0, 0, 0};      // descriptors of each class
-    size_t smem[kClasses] = {0, 0, 0};
+    int off[kClasses] = {0, 0, 0, 0};  // first descriptor of each class
+    int n[kClasses] = {0, 0, 0, 0};    // descriptors of each class
+    size_t smem[kClasses] = {0, 0, 0, 0};
     int total = 0;
 };
 
@@ -259,19 +366,36 @@ static bool launch_class(const DevBatch &db, int c, cudaStream_t st) {
     return cuda_ok(cudaGetLastError(), "k_batch launch");
 }
 
+static bool launch_cols(const DevBatch &db, cudaStream_t st) {
+    Device *d = device();
+    static bool attr = false;
+    if (!attr) {
+        if (!cuda_ok(cudaFuncSetAttribute(k_batch_cols, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)d->smem_optin - 512),
+                     "cudaFuncSetAttribute"))
+            return false;
+        attr = true;
+    }
+    const int c = kColClass;
+    k_batch_cols<<<db.n[c] * kColCluster, BT, db.smem[c], st>>>(db.q + db.off[c], db.n[c]);
+    count_launch();
+    return cuda_ok(cudaGetLastError(), "k_batch_cols launch");
+}
+
 static bool launch_one(const DevBatch &db, int c, cudaStream_t st) {
     switch (c) {
         case 0: return launch_class<256>(db, c, st);
         case 1: return launch_class<512>(db, c, st);
-        default: return launch_class<1024>(db, c, st);
+        case 2: return launch_class<1024>(db, c, st);
+        default: return launch_cols(db, st);
     }
 }
 
 // Streams and events the classes run on side by side (forked from and joined
 // back to the caller's stream; the same pattern is recorded into the graph).
 struct BatchStreams {
-    cudaStream_t s[kClasses] = {nullptr, nullptr, nullptr};
-    cudaEvent_t fork = nullptr, join[kClasses] = {nullptr, nullptr, nullptr};
+    cudaStream_t s[kClasses] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t fork = nullptr, join[kClasses] = {nullptr, nullptr, nullptr, nullptr};
     bool ready = false;
 };
 static BatchStreams g_bs;

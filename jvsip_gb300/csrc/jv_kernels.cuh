@@ -433,9 +433,11 @@ __host__ __device__ __forceinline__ int pass_count(unsigned long long packed, in
     return (int)((packed >> (4 * i)) & 15ull);
 }
 
-template <typename T, int R, int EMAX>
+template <typename T, int R, int EMAX, bool DIN = false>
 __device__ __forceinline__ void smem_pass(typename cplx_t<T>::t *s, int ld, int nt, int Ns,
                                           const typename cplx_t<T>::t *__restrict__ tp, const uint4 pc) {
+    // DIN: the pass reads a dense (unpadded) row -- the first pass over data
+    // that arrived in shared memory in natural order
     // tp: this pass's twiddles, entry r*Ns + m = exp(-2 pi i r m/(Ns R)), so the
     // threads of a warp (consecutive m) read consecutive entries; pc: NR = N/R,
     // the multiply-high magic numbers of NR and Ns
@@ -453,7 +455,7 @@ __device__ __forceinline__ void smem_pass(typename cplx_t<T>::t *s, int ld, int 
             int t = mdiv(b, mNR), j = b - t * NR;
             const C *src = s + t * ld;
 #pragma unroll
-            for (int r = 0; r < R; r++) v[k][r] = src[spad(j + r * NR)];
+            for (int r = 0; r < R; r++) v[k][r] = src[DIN ? (j + r * NR) : spad(j + r * NR)];
         }
     }
     __syncthreads();
