@@ -18,6 +18,8 @@ matrix.
                reference's own sources do not exist on the GPU host) on all
                host threads over a bounded sample of the same rows; this leg
                also checks sampled GPU rows against the FP64 oracle.
+  forms        (one GPU) the precision form (cfg4) and the batching form (cfg5)
+               against the plain kernel, each from its own bench.py run.
 
 Other configurations (--workload): cfg1 (64x1024), cfg2col (1000-point
 columns x 4096), cfg2rc / cfg2cr (4096 x 1536 real <-> 4096 x 769), cfg3d
@@ -61,6 +63,8 @@ def args():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU-baseline sample (wall seconds)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="default workload: skip the precision-form and batching-form summaries")
     ap.add_argument("--no-autotune", action="store_true",
                     help="cfg5: use the cached or heuristic tiling (profiling runs: no tuner launches)")
     ap.add_argument("--batch-gb", type=float, default=2.0, help="cfg5: bytes per buffer of the instance sequence (0: the literal 20000 instances)")
@@ -471,6 +475,37 @@ def batching_workload(a, torch, J, L, ext):
 
 
 # ---------------------------------------------------------------- default workload
+def forms_summary(a):
+    """The precision form (cfg4: plain against split FP16 / BF16 on 32768x1024,
+    rows scaled by 10^U(-3,3)) and the batching form (cfg5: the 2 GB instance
+    sequence, one graph replay against a loop of per-plan calls), each measured
+    by its own bench.py run on the same GPU, summarised for the default line."""
+    out = {}
+    runs = (("cfg4", ["--cpu-seconds", "2"]), ("cfg5", ["--no-cpu"]))
+    for wl, extra in runs:
+        cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--workload", wl, "--steps", "20", "--warmup", "5"]
+        try:
+            r = subprocess.run(cmd + extra, capture_output=True, text=True, timeout=900)
+            d = json.loads(r.stdout.strip().splitlines()[-1])
+        except Exception as e:  # reported, never fatal for the main line
+            out[wl] = {"error": str(e)[-300:]}
+            continue
+        if wl == "cfg4":
+            f = d.get("forms", {})
+            out["precision_form"] = {
+                "workload": d["config"]["workload"], "unit": "GB/s",
+                "plain": {"value": d["value"], "rel_l2_vs_fp64_oracle": d.get("rel_l2_vs_fp64_oracle")},
+                "split_fp16": f.get("split_fp16"), "split_bf16": f.get("split_bf16"),
+                "hbm_frac_plain": d.get("hbm_frac")}
+        else:
+            out["batching_form"] = {
+                "workload": d["config"]["workload"], "unit": "GB/s",
+                "batched": {"value": d["value"], "ms_per_step": d["ms_per_step"], "gpu_launches": d.get("gpu_launches")},
+                "plain_loop": d.get("plain_loop"), "batched_over_loop": d.get("batched_over_loop"),
+                "rel_l2_vs_fp64_numpy_sampled": d.get("rel_l2_vs_fp64_numpy_sampled"), "hbm_frac": d.get("hbm_frac")}
+    return out
+
+
 def main():
     a = args()
     if a.impl == "reference":
@@ -625,6 +660,8 @@ def main():
     }
     if line["cpu_baseline"]:
         line["rel_l2_vs_fp64_oracle"] = line["cpu_baseline"].get("gpu_rel_l2_vs_fp64_oracle")
+    if not a.no_forms and world == 1:
+        line["forms"] = forms_summary(a)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
