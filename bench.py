@@ -238,6 +238,21 @@ def timed_calls(torch, ext, call, steps, flush=None):
     return per
 
 
+def max_over_ranks(torch, dist, ms, device="cuda"):
+    """The largest per-rank time (ms) over all ranks (the job's time); the
+    rank's own time without a process group."""
+    if dist is None:
+        return ms
+    t = torch.tensor([float(ms)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_gbs(bytes_per_rank, world, ms):
+    """Whole-job GB/s: every rank moves bytes_per_rank in ms (replicas, weak scaling)."""
+    return bytes_per_rank * world / (ms / 1e3) / 1e9
+
+
 def link_time(torch, hin, hout, reps=3):
     """ms to copy hin host->device and, at the same time, a device buffer of
     hout's size device->host (pinned memory, two streams): the host-link bound
@@ -567,13 +582,9 @@ def main():
     launches = L.jvsip_gpu_kernel_launches() - n0
     J.check("timed loop")
     per = [ev[i].elapsed_time(ev[i + 1]) for i in range(a.steps)]
-    total_ms = ev[0].elapsed_time(ev[a.steps])
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(torch, dist, ev[0].elapsed_time(ev[a.steps]))
     ms_per_step = total_ms / a.steps
-    value = nbytes * world / (ms_per_step / 1e3) / 1e9
+    value = job_gbs(nbytes, world, ms_per_step)
     by.sync()
 
     # end to end: the same call on pinned host user blocks that are not admitted
@@ -599,16 +610,12 @@ def main():
         torch.cuda.synchronize()
         wall = time.perf_counter() - w0
         J.check("e2e loop")
-        ems = max(e0.elapsed_time(e1) / a.steps, 1000 * wall / a.steps)
-        if dist:
-            t = torch.tensor([ems], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ems = float(t.item())
+        ems = max_over_ranks(torch, dist, max(e0.elapsed_time(e1) / a.steps, 1000 * wall / a.steps))
         ye_np = ye.numpy()
         k = 2 * N * min(64, M)
         diff = float(np.abs(ye_np[:k] - y_np[:k]).max())
         link_ms = link_time(torch, xe, ye)  # overwrites ye
-        e2e = {"value": round(nbytes * world / (ems / 1e3) / 1e9, 2), "unit": "GB/s",
+        e2e = {"value": round(job_gbs(nbytes, world, ems), 2), "unit": "GB/s",
                "h2d_bytes_per_step": n2 * 4, "d2h_bytes_per_step": n2 * 4, "ms_per_step": round(ems, 3),
                "path": "vsip_ccfftmop_f on pinned, non-admitted user blocks (staged inside the call)",
                "max_abs_diff_vs_resident": diff,
