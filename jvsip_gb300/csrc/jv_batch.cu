@@ -62,7 +62,8 @@ __device__ __forceinline__ void batch_tile(const TileDesc &d, float2 *s) {
     io.in_vs = d.in_vs;
     io.out_es = d.out_es;
     io.out_vs = d.out_vs;
-    io.sgn = d.inv ? -1.f : 1.f;
+    io.smask = d.inv ? 0x80000000u : 0u;
+    io.has_scale = d.has_scale != 0;
     io.scale = d.has_scale ? d.scale : 1.f;
     io.vf = d.vec_fast != 0;
     io.mnt = d.mnt;

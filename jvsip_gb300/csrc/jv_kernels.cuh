@@ -503,13 +503,34 @@ __device__ __forceinline__ void smem_passes(typename cplx_t<T>::t *s, int ld, in
 // between passes.  Butterfly b of the tile maps to (transform t, index j):
 // j fastest for row tiles (consecutive threads read consecutive elements),
 // t fastest for column tiles (consecutive threads read adjacent transforms).
+// x with its sign bit flipped when m = 0x80000000 (exact negation on the
+// integer pipe; m = 0 leaves x unchanged)
+__device__ __forceinline__ float flip_sign(float x, unsigned m) { return __int_as_float(__float_as_int(x) ^ (int)m); }
+__device__ __forceinline__ double flip_sign(double x, unsigned m) {
+    return __longlong_as_double(__double_as_longlong(x) ^ ((long long)m << 32));
+}
+
+// the stored value: conjugated back for the inverse, scaled when the plan has a
+// scale (single precision multiplies by 1 otherwise, which is exact; double
+// precision, bound by its FP64 pipe, skips the multiply)
+template <typename C, typename T>
+__device__ __forceinline__ C out_value(C v, unsigned smask, bool has_scale, T scale) {
+    v.y = flip_sign(v.y, smask);
+    if (sizeof(T) == 4 || has_scale) {
+        v.x *= scale;
+        v.y *= scale;
+    }
+    return v;
+}
+
 template <typename T> struct TileIO {
     typedef typename cplx_t<T>::t C;
     const C *in;     // interleaved input; element (t, n) at in[t*in_vs + n*in_es]
     C *out;          // interleaved output; element (t, n) at out[t*out_vs + n*out_es]
     long in_es, in_vs, out_es, out_vs;
-    T sgn;           // -1: inverse (conjugate on load and on store), else +1
-    T scale;         // 1 when the plan has no scale (x * 1 is exact)
+    unsigned smask;  // 0x80000000: inverse (conjugate on load and on store), else 0
+    bool has_scale;
+    T scale;         // 1 when the plan has no scale
     bool vf;         // t-fastest mapping
     unsigned mnt;    // multiply-high magic of the tile's transform count
 };
@@ -545,7 +566,7 @@ __device__ __forceinline__ void pass_first(typename cplx_t<T>::t *s, int ld, int
 #pragma unroll
             for (int r = 0; r < R; r++) {
                 C c = src[r * st];
-                c.y *= io.sgn;
+                c.y = flip_sign(c.y, io.smask);
                 v[k][r] = c;
             }
         }
@@ -560,9 +581,8 @@ __device__ __forceinline__ void pass_first(typename cplx_t<T>::t *s, int ld, int
             if (LAST) {
                 // one pass: N = R, j = 0, output element r
                 C *dst = io.out + (long)t * io.out_vs;
-                const T sy = io.sgn * io.scale;
 #pragma unroll
-                for (int r = 0; r < R; r++) dst[r * io.out_es] = mk<C>(v[k][r].x * io.scale, v[k][r].y * sy);
+                for (int r = 0; r < R; r++) dst[r * io.out_es] = out_value(v[k][r], io.smask, io.has_scale, io.scale);
             } else {
                 C *dst = s + t * ld;
 #pragma unroll
@@ -594,7 +614,6 @@ __device__ __forceinline__ void pass_last(const typename cplx_t<T>::t *s, int ld
             for (int r = 0; r < R; r++) v[k][r] = src[spad(j + r * NR)];
         }
     }
-    const T sy = io.sgn * io.scale;
 #pragma unroll
     for (int k = 0; k < K; k++) {
         const int b = tid + k * nthr;
@@ -609,7 +628,7 @@ __device__ __forceinline__ void pass_last(const typename cplx_t<T>::t *s, int ld
             C *dst = io.out + ((long)t * io.out_vs + (long)j * io.out_es);
             const long st = (long)Ns * io.out_es;
 #pragma unroll
-            for (int r = 0; r < R; r++) dst[r * st] = mk<C>(v[k][r].x * io.scale, v[k][r].y * sy);
+            for (int r = 0; r < R; r++) dst[r * st] = out_value(v[k][r], io.smask, io.has_scale, io.scale);
         }
     }
 }
@@ -789,7 +808,8 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
             io.in_vs = cin.vs;
             io.out_es = cout.es;
             io.out_vs = cout.vs;
-            io.sgn = a.inv ? (T)-1 : (T)1;
+            io.smask = a.inv ? 0x80000000u : 0u;
+            io.has_scale = a.has_scale != 0;
             io.scale = a.has_scale ? a.scale : (T)1;
             io.vf = a.vec_fast != 0;
             io.mnt = (nt == a.vpb) ? a.mvpb : magic_of((unsigned)nt);
@@ -813,7 +833,8 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
             io.in_es = 1;
             io.in_vs = rin.vs / 2;
             io.out_es = io.out_vs = 0;
-            io.sgn = (T)1;
+            io.smask = 0u;
+            io.has_scale = false;
             io.scale = (T)1;
             io.vf = false;
             io.mnt = 0;
@@ -865,7 +886,8 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
             io.in_es = io.in_vs = 0;
             io.out_es = 1;
             io.out_vs = rout.vs / 2;
-            io.sgn = (T)-1;
+            io.smask = 0x80000000u;
+            io.has_scale = a.has_scale != 0;
             io.scale = a.has_scale ? a.scale : (T)1;
             io.vf = false;
             io.mnt = 0;
