@@ -82,22 +82,6 @@ __device__ __forceinline__ void mbar_init(void *mbar, uint32_t count) {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-// one arrival of this thread (release semantics at CTA scope)
-__device__ __forceinline__ void mbar_arrive(void *mbar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_addr(mbar)) : "memory");
-}
-
-// one test of the barrier phase of parity `phase` (acquire when it succeeds)
-__device__ __forceinline__ bool mbar_try(void *mbar, uint32_t phase) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done) : "r"(smem_addr(mbar)), "r"(phase) : "memory");
-    return done != 0;
-}
-
 // Wait for the barrier phase with an iteration limit; returns false when the
 // limit expired (the caller records an error and leaves without using the result).
 __device__ __forceinline__ bool mbar_wait(void *mbar, uint32_t phase, uint32_t limit) {
