@@ -288,6 +288,13 @@ unsigned long jvsip_gpu_kernel_launches(void);
  * kept for parity checks (returns the map length). */
 int  jvsip_fftm_passes(const void *plan, int *radix, int cap);
 long jvsip_fftm_jofk(const void *plan, unsigned long *out, long cap);
+/* Number of calls of the plan held as captured CUDA graphs (no counterpart in
+ * the reference).  A plan created with ntimes == 0 ("used many times")
+ * captures the launch sequence of a device-resident call the second time it
+ * sees the call's views and replays it afterwards (at most 8 per plan, the
+ * oldest dropped); other plans and staged calls launch directly.  -1 for an
+ * invalid plan. */
+int  jvsip_fftm_graphs(const void *plan);
 
 /* Complex-to-complex multiple FFT that allocates nothing (no counterpart in
  * the reference).  For callers that cannot allocate device memory when they

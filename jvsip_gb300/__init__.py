@@ -48,7 +48,7 @@ EXPORTS = [
     "jvsip_cblocksync_f", "jvsip_cblocksync_d", "jvsip_blocksync_f", "jvsip_blocksync_d",
     "jvsip_fftm_setform_f", "jvsip_fftm_getform_f",
     "jvsip_fftm_batch_f", "jvsip_fftm_batch_create_f", "jvsip_fftm_batch_run_f", "jvsip_fftm_batch_destroy_f",
-    "jvsip_gpu_build_info", "jvsip_gpu_synchronize", "jvsip_gpu_stream", "jvsip_fftm_passes", "jvsip_fftm_jofk",
+    "jvsip_gpu_build_info", "jvsip_gpu_synchronize", "jvsip_gpu_stream", "jvsip_fftm_passes", "jvsip_fftm_jofk", "jvsip_fftm_graphs",
     "jvsip_gpu_kernel_launches", "jvsip_ccfftm_noalloc_f", "jvsip_fftm_autotune_f",
     "jvsip_fftm_autotune_entries",
 ]
@@ -151,6 +151,8 @@ def lib(load_only: bool = False):
     L.jvsip_fftm_batch_run_f.argtypes = [vp]
     L.jvsip_fftm_batch_destroy_f.argtypes = [vp]
     L.jvsip_fftm_passes.argtypes = [vp, C.POINTER(C.c_int), C.c_int]
+    L.jvsip_fftm_graphs.argtypes = [vp]
+    L.jvsip_fftm_graphs.restype = C.c_int
     L.jvsip_fftm_jofk.restype = C.c_long
     L.jvsip_fftm_jofk.argtypes = [vp, C.POINTER(C.c_ulong), C.c_long]
     _lib = L

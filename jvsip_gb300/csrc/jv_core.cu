@@ -78,6 +78,7 @@ Device *device() {
 // ------------------------------------------------------------------ launch counter
 static std::atomic<unsigned long long> g_launches{0};
 void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+void count_launch_undo(unsigned long long n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
 
 // ------------------------------------------------------------------ memory pool
 static std::mutex g_pool_mu;

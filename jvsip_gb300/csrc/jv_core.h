@@ -110,6 +110,17 @@ struct Job {
     bool no_pipeline = false;  // JVSIP_GPU_NO_PIPELINE at plan creation: one staging copy each way
 };
 
+// A device-resident call of a plan captured into a CUDA graph: plans created
+// with ntimes == 0 ("many times") capture the launch sequence of a call the
+// second time they see its views and replay it afterwards.
+struct CallGraph {
+    Job key;                        // the resolved call
+    cudaGraphExec_t exec = nullptr;
+    unsigned kernels = 0;           // kernel launches the graph holds
+    bool failed = false;            // capture was refused: run directly
+};
+void count_launch_undo(unsigned long long n);  // launches recorded by a capture did not run
+
 // Kernel entry points (defined in the kernel translation units).
 bool launch_smem_f32(const Job &j, cudaStream_t s);
 bool launch_smem_f64(const Job &j, cudaStream_t s);
@@ -146,6 +157,7 @@ struct Plan {
     void *d_twg = nullptr;    // per-pass [r][m] twiddle tables of the general kernel's schedule
     void *d_pc = nullptr;     // per-pass constants of that schedule (PassConst, one per pass)
     std::vector<unsigned long> jofk;  // reference digit-reversal map (kept for parity checks)
+    std::vector<CallGraph> graphs;    // captured calls (ntimes == 0), most recent last
     std::mutex mu;            // the plan is used by one call at a time
 };
 

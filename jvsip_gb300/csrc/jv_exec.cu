@@ -241,8 +241,9 @@ static void mark_written(const void *blk) {
 }
 
 // ---------------------------------------------------------------- dispatch
-static bool run_job(Job &j, cudaStream_t st) {
-    if (j.nvec <= 0 || j.N <= 0) return true;
+// true when the call runs in one of the shared-memory / register kernels (no
+// scratch allocation); false for the multi-pass global path
+static bool job_in_smem(const Job &j) {
     long lim = smem_max_len(j.prec, j.kind);
     bool smooth = true;
     for (int i = 0; i < j.npass; i++) {
@@ -252,10 +253,15 @@ static bool run_job(Job &j, cudaStream_t st) {
     }
     if (!j.twg || !j.pc) smooth = false;
     long need = j.N + (j.kind == K_C2R ? 1 : 0);
+    return smooth && need <= lim;
+}
+
+static bool run_job(Job &j, cudaStream_t st) {
+    if (j.nvec <= 0 || j.N <= 0) return true;
     if (j.form == JVSIP_FORM_SPLIT_BF16 || j.form == JVSIP_FORM_SPLIT_FP16) {
         if (launch_split_f32(j, st)) return jvsip_gpu_last_error() == 0;
     }
-    if (smooth && need <= lim) {
+    if (job_in_smem(j)) {
         if (j.prec == P_F32) {
             if (launch_fast_f32(j, st)) return true;
             return launch_smem_f32(j, st);
@@ -263,6 +269,75 @@ static bool run_job(Job &j, cudaStream_t st) {
         return launch_smem_f64(j, st);
     }
     return j.prec == P_F32 ? launch_global_f32(j, st) : launch_global_f64(j, st);
+}
+
+// ---------------------------------------------------------------- plan graphs
+static bool same_cview(const CView &a, const CView &b) {
+    return a.re == b.re && a.im == b.im && a.cst == b.cst && a.off == b.off && a.es == b.es && a.vs == b.vs;
+}
+static bool same_rview(const RView &a, const RView &b) {
+    return a.a == b.a && a.rst == b.rst && a.off == b.off && a.es == b.es && a.vs == b.vs;
+}
+static bool same_call(const Job &a, const Job &b) {
+    return a.kind == b.kind && a.form == b.form && a.no_fast == b.no_fast && a.inplace == b.inplace &&
+           a.nvec == b.nvec && same_cview(a.cin, b.cin) && same_cview(a.cout, b.cout) && same_rview(a.rin, b.rin) &&
+           same_rview(a.rout, b.rout);
+}
+
+// A device-resident call of a plan created with ntimes == 0: the first call
+// with these views runs directly (and creates every lazily built resource),
+// the second is captured into a CUDA graph, later ones replay it.  Calls on
+// the multi-pass global path (scratch allocations) always run directly.
+static constexpr size_t kPlanGraphs = 8;
+
+static bool run_job_planned(Plan *p, Job &j, cudaStream_t st) {
+    if (p->ntimes != 0 || j.nvec <= 0 || j.N <= 0) return run_job(j, st);
+    const bool split = (j.form == JVSIP_FORM_SPLIT_BF16 || j.form == JVSIP_FORM_SPLIT_FP16);
+    if (!split && !job_in_smem(j)) return run_job(j, st);
+    CallGraph *e = nullptr;
+    for (CallGraph &g : p->graphs)
+        if (same_call(g.key, j)) e = &g;
+    if (!e) {
+        if (p->graphs.size() >= kPlanGraphs) {
+            if (p->graphs.front().exec) cudaGraphExecDestroy(p->graphs.front().exec);
+            p->graphs.erase(p->graphs.begin());
+        }
+        CallGraph g;
+        g.key = j;
+        p->graphs.push_back(g);
+        return run_job(j, st);
+    }
+    if (!e->exec && !e->failed) {
+        cudaStream_t cs = nullptr;
+        cudaGraph_t graph = nullptr;
+        const int err0 = jvsip_gpu_last_error();
+        const unsigned long n0 = jvsip_gpu_kernel_launches();
+        bool ok = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        bool ran = false;
+        if (ok) {
+            ran = run_job(j, cs);
+            ok = (cudaStreamEndCapture(cs, &graph) == cudaSuccess) && ran && graph;
+        }
+        const unsigned long n1 = jvsip_gpu_kernel_launches();
+        count_launch_undo(n1 - n0);  // recorded, not run
+        if (ok) ok = cudaGraphInstantiate(&e->exec, graph, 0) == cudaSuccess;
+        if (graph) cudaGraphDestroy(graph);
+        if (cs) cudaStreamDestroy(cs);
+        e->kernels = (unsigned)(n1 - n0);
+        if (!ok) {
+            cudaGetLastError();
+            if (e->exec) cudaGraphExecDestroy(e->exec);
+            e->exec = nullptr;
+            e->failed = true;
+            // an error recorded by the refused capture is not the caller's
+            if (err0 == 0 && jvsip_gpu_last_error() != 0) jvsip_gpu_clear_error();
+        }
+    }
+    if (!e->exec) return run_job(j, st);
+    if (!cuda_ok(cudaGraphLaunch(e->exec, st), "plan graph launch")) return false;
+    count_launch(e->kernels);
+    return true;
 }
 
 // Staged (host) views: copy results back and wait, so the host data is
@@ -443,7 +518,7 @@ static void exec_cc(const VP *vp, const CMV *x, const CMV *y, bool ip) {
             j.cin.off -= xl;
         }
     }
-    bool ok = run_job(j, st);
+    bool ok = (stg.regs.empty() && !tmp) ? run_job_planned(p, j, st) : run_job(j, st);
     ok = finish(stg, st, ok);
     dfree(tmp);  // stream-ordered: the pool hands it out only to later work on this stream
     if (ok) mark_written(same_view ? (const void *)x->block : (const void *)y->block);
@@ -480,7 +555,7 @@ static void exec_rc(const VP *vp, const RMV *x, const CMV *z) {
     if (!stg.upload(st)) return;
     j.rin = dev_r(stg, rx);
     j.cout = dev_c(stg, rz);
-    bool ok = run_job(j, st);
+    bool ok = stg.regs.empty() ? run_job_planned(p, j, st) : run_job(j, st);
     ok = finish(stg, st, ok);
     if (ok) mark_written(z->block);
 }
@@ -516,7 +591,7 @@ static void exec_cr(const VP *vp, const CMV *z, const RMV *x) {
     if (!stg.upload(st)) return;
     j.cin = dev_c(stg, rz);
     j.rout = dev_r(stg, rx);
-    bool ok = run_job(j, st);
+    bool ok = stg.regs.empty() ? run_job_planned(p, j, st) : run_job(j, st);
     ok = finish(stg, st, ok);
     if (ok) {
         if (rx.blk->parent) mark_written(rx.blk->parent);

@@ -320,6 +320,8 @@ static void plan_free(Plan *p) {
     if (!p) return;
     Device *d = device();
     if (d) cudaStreamSynchronize(d->stream);
+    for (CallGraph &g : p->graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
     release_tables(p);
     delete p;
 }
@@ -496,6 +498,14 @@ int jvsip_fftm_passes(const void *vp, int *radix, int cap) {
     if (!p) return -1;
     int n = (int)p->radix.size();
     for (int i = 0; i < n && i < cap; i++) radix[i] = p->radix[i];
+    return n;
+}
+int jvsip_fftm_graphs(const void *vp) {
+    Plan *p = plan_of(vp);
+    if (!p) return -1;
+    std::lock_guard<std::mutex> lk(p->mu);
+    int n = 0;
+    for (const CallGraph &g : p->graphs) n += g.exec ? 1 : 0;
     return n;
 }
 long jvsip_fftm_jofk(const void *vp, unsigned long *out, long cap) {
