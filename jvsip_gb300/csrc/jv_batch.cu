@@ -108,7 +108,7 @@ __device__ __forceinline__ void col_passes(float2 *s, int ld, unsigned long long
     while (fi < kRadices - 1 && pass_count(packed, fi) == 0) fi++;
     const uint4 pc0 = __ldg(&pc[0]);
     int Rf = 2;
-#define JV_DENSE_FIRST(R) (smem_pass<float, R, BEMAX, true>(s, ld, 1, 1, twg, pc0), Rf = R)
+#define JV_DENSE_FIRST(R) (smem_pass<float, R, BEMAX, 1>(s, ld, 1, 1, twg, pc0), Rf = R)
     JV_RADIX_SWITCH(fi, JV_DENSE_FIRST)
 #undef JV_DENSE_FIRST
     int Ns = Rf, p = 1;

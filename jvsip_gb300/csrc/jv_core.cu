@@ -80,6 +80,34 @@ static std::atomic<unsigned long long> g_launches{0};
 void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 void count_launch_undo(unsigned long long n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
 
+// Device status word of the kernels that wait on asynchronous copies (the
+// TMA-staged column tiles): set to 1 when a bounded wait expired.
+static std::mutex g_ks_mu;
+static int *g_ks = nullptr;
+int *kernel_status() {
+    std::lock_guard<std::mutex> lk(g_ks_mu);
+    if (!g_ks) {
+        g_ks = (int *)dmalloc(sizeof(int));
+        if (g_ks && cudaMemset(g_ks, 0, sizeof(int)) != cudaSuccess) g_ks = nullptr;
+    }
+    return g_ks;
+}
+int kernel_status_check(cudaStream_t st) {
+    std::lock_guard<std::mutex> lk(g_ks_mu);
+    if (!g_ks) return 0;
+    int h = 0;
+    if (cudaMemcpyAsync(&h, g_ks, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return E_CUDA;
+    if (h) {
+        cudaMemsetAsync(g_ks, 0, sizeof(int), st);
+        set_error(E_DEVICE, "a bounded wait for an asynchronous tile copy expired");
+        return E_DEVICE;
+    }
+    return 0;
+}
+
+
 // ------------------------------------------------------------------ memory pool
 static std::mutex g_pool_mu;
 static std::multimap<size_t, void *> g_free;       // size -> buffer
@@ -235,7 +263,9 @@ int jvsip_gpu_synchronize(void) {
     Device *d = device();
     if (!d) return E_NODEVICE;
     if (!cuda_ok(cudaStreamSynchronize(d->stream), "cudaStreamSynchronize")) return E_CUDA;
-    return split_status_check(d->stream);
+    const int k = jv::kernel_status_check(d->stream);
+    const int sp = split_status_check(d->stream);
+    return k ? k : sp;
 }
 
 int vsip_init(void *ptr) {

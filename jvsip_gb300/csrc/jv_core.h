@@ -108,6 +108,8 @@ struct Job {
     int form = 0;        // JVSIP_FORM_* of the plan
     bool no_fast = false;      // JVSIP_GPU_NO_FAST at plan creation: general kernels only
     bool no_pipeline = false;  // JVSIP_GPU_NO_PIPELINE at plan creation: one staging copy each way
+    int tma_columns = -1;      // JVSIP_GPU_TMA_COLUMNS at plan creation: 1 / 0 force TMA-staged
+                               // column tiles on / off, -1 (unset) automatic
 };
 
 // A device-resident call of a plan captured into a CUDA graph: plans created
@@ -132,6 +134,8 @@ bool launch_fast_f32(const Job &j, cudaStream_t s);   // specialised kernels; fa
 std::vector<int> fast_radices(long N);                // radix list of the specialised kernel for N
 bool launch_split_f32(const Job &j, cudaStream_t s);  // precision form; false when the call does not qualify
 int split_status_check(cudaStream_t s);               // device status of the precision form (0 = clean)
+int *kernel_status();                                 // device word a kernel sets when a bounded wait expired
+int kernel_status_check(cudaStream_t s);              // reads and clears it (0 = clean)
 
 // Capacity queries used by the dispatcher.
 long smem_max_len(int prec, int kind);   // largest N the shared-memory kernel takes
@@ -149,6 +153,7 @@ struct Plan {
     int form = 0;             // JVSIP_FORM_*
     bool no_fast = false;     // environment switches read once at creation
     bool no_pipeline = false;
+    int tma_columns = -1;
     std::vector<int> radix;   // pass radices of the device kernels (product = MN)
     bool smooth = true;       // every radix is one of the built-in codelets
     void *d_tw = nullptr;     // forward twiddles, MN entries

@@ -279,7 +279,8 @@ static bool same_rview(const RView &a, const RView &b) {
     return a.a == b.a && a.rst == b.rst && a.off == b.off && a.es == b.es && a.vs == b.vs;
 }
 static bool same_call(const Job &a, const Job &b) {
-    return a.kind == b.kind && a.form == b.form && a.no_fast == b.no_fast && a.inplace == b.inplace &&
+    return a.kind == b.kind && a.form == b.form && a.no_fast == b.no_fast && a.tma_columns == b.tma_columns &&
+           a.inplace == b.inplace &&
            a.nvec == b.nvec && same_cview(a.cin, b.cin) && same_cview(a.cout, b.cout) && same_rview(a.rin, b.rin) &&
            same_rview(a.rout, b.rout);
 }
@@ -365,6 +366,7 @@ static void fill_job(Job &j, const Plan *p, int kind) {
     j.form = p->form;
     j.no_fast = p->no_fast;
     j.no_pipeline = p->no_pipeline;
+    j.tma_columns = p->tma_columns;
     j.npass = (int)p->radix.size();
     for (int i = 0; i < j.npass && i < 40; i++) j.radix[i] = p->radix[i];
 }

@@ -15,8 +15,11 @@
 // the conjugations folded into the load and store of each element.
 #pragma once
 
+#include <cuda.h>  // CUtensorMap
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include "jv_tc.cuh"
 
 #include "jv_core.h"
 
@@ -411,6 +414,12 @@ template <typename T> struct SmemArgs {
     const uint4 *pc;  // per-pass constants of the schedule (NR, magic NR, Ns, magic Ns)
     unsigned mvpb;    // multiply-high magic of vpb
     int real_pairs;   // R2C input / C2R output rows: unit stride, even offset and pitch, 2-element aligned
+    // column tiles of c2c loaded by TMA: boxes of (2*vpb scalars) x tma_rows
+    // rows of the input view (tmap), tma_boxes per tile, tma_bytes in all
+    int tma, tma_boxes, tma_rows;
+    unsigned tma_bytes;
+    int *status;      // set to 1 when the bounded wait for the boxes expired
+    CUtensorMap tmap;
     WalkConst win, wout;  // load / store walker constants for full tiles of vpb transforms
     CAcc<T> cin;
     CSto<T> cout;
@@ -433,11 +442,13 @@ __host__ __device__ __forceinline__ int pass_count(unsigned long long packed, in
     return (int)((packed >> (4 * i)) & 15ull);
 }
 
-template <typename T, int R, int EMAX, bool DIN = false>
+template <typename T, int R, int EMAX, int IN = 0>
 __device__ __forceinline__ void smem_pass(typename cplx_t<T>::t *s, int ld, int nt, int Ns,
-                                          const typename cplx_t<T>::t *__restrict__ tp, const uint4 pc) {
-    // DIN: the pass reads a dense (unpadded) row -- the first pass over data
-    // that arrived in shared memory in natural order
+                                          const typename cplx_t<T>::t *__restrict__ tp, const uint4 pc, int dp = 0) {
+    // IN: where the pass reads -- 0 the padded rows; 1 dense rows (t*ld + n);
+    // 2 dense transposed (n*dp + t), the order a TMA box of adjacent
+    // transforms lands in (the first pass over data that arrived in natural
+    // order; the pass writes the padded rows in place)
     // tp: this pass's twiddles, entry r*Ns + m = exp(-2 pi i r m/(Ns R)), so the
     // threads of a warp (consecutive m) read consecutive entries; pc: NR = N/R,
     // the multiply-high magic numbers of NR and Ns
@@ -455,7 +466,8 @@ __device__ __forceinline__ void smem_pass(typename cplx_t<T>::t *s, int ld, int 
             int t = mdiv(b, mNR), j = b - t * NR;
             const C *src = s + t * ld;
 #pragma unroll
-            for (int r = 0; r < R; r++) v[k][r] = src[DIN ? (j + r * NR) : spad(j + r * NR)];
+            for (int r = 0; r < R; r++)
+                v[k][r] = (IN == 2) ? s[(j + r * NR) * dp + t] : src[IN == 1 ? (j + r * NR) : spad(j + r * NR)];
         }
     }
     __syncthreads();
@@ -705,6 +717,35 @@ __device__ __forceinline__ void c2c_tile(typename cplx_t<T>::t *s, int ld, int n
     tile_passes<T, EMAX, true, true>(s, ld, nt, packed, twg, pc, io);
 }
 
+// A c2c tile whose input arrived in shared memory as n*dp + t (TMA boxes of
+// adjacent transforms): the first pass reads that order, the last pass
+// writes the view.  The schedule must have at least two passes.
+template <typename T, int EMAX>
+__device__ __forceinline__ void staged_tile(typename cplx_t<T>::t *s, int ld, int nt, int dp, unsigned long long packed,
+                                            const typename cplx_t<T>::t *__restrict__ twg,
+                                            const uint4 *__restrict__ pc, const TileIO<T> &io) {
+    typedef typename cplx_t<T>::t C;
+    int fi = -1, li = 0;
+    for (int i = 0; i < kRadices; i++)
+        if (pass_count(packed, i)) {
+            if (fi < 0) fi = i;
+            li = i;
+        }
+    const uint4 pc0 = __ldg(&pc[0]);
+    int Rf = 2;
+#define JV_STAGED_FIRST(R) (smem_pass<T, R, EMAX, 2>(s, ld, nt, 1, twg, pc0, dp), Rf = R)
+    JV_RADIX_SWITCH(fi, JV_STAGED_FIRST)
+#undef JV_STAGED_FIRST
+    int Ns = Rf, p = 1;
+    const C *tp = twg + Rf;
+    const unsigned long long mid = packed - (1ull << (4 * fi)) - (1ull << (4 * li));
+    smem_passes_from<T, EMAX>(s, ld, nt, mid, tp, pc, Ns, p);
+    const uint4 pcl = __ldg(&pc[p]);
+#define JV_LAST(R) pass_last<T, R, EMAX>(s, ld, nt, Ns, tp, pcl, io)
+    JV_RADIX_SWITCH(li, JV_LAST)
+#undef JV_LAST
+}
+
 // smem_passes starting from pass p with Ns and the table pointer tp (updated)
 template <typename T, int EMAX>
 __device__ __forceinline__ void smem_passes_from(typename cplx_t<T>::t *s, int ld, int nt, unsigned long long packed,
@@ -779,9 +820,9 @@ __device__ __forceinline__ void tile_load(Walk &w, bool vf, int tot, C *s, int l
 }
 
 template <typename T, int KIND, int EMAX, int MAXT>
-__global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
+__global__ void __launch_bounds__(MAXT) k_smem(const __grid_constant__ SmemArgs<T> a) {
     typedef typename cplx_t<T>::t C;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     C *s = reinterpret_cast<C *>(smem_raw);
     const int N = a.N, ld = a.ld;
     // register copies: member calls on kernel-parameter structs would force local copies
@@ -802,6 +843,40 @@ __global__ void __launch_bounds__(MAXT) k_smem(const SmemArgs<T> a) {
         if (KIND == K_C2C && a.passes != 0 && cin.vec && cout.vec) {
             // c2c on interleaved views: first pass from the view, last pass to the view
             TileIO<T> io;
+            if (a.tma) {
+                // column tile: TMA boxes of the vpb adjacent transforms land as n*vpb + t
+                __shared__ __align__(8) uint64_t tbar;
+                if (tid == 0) tc::mbar_init(&tbar, 1);
+                __syncthreads();
+                if (tid == 0) {
+                    tc::mbar_expect_tx(&tbar, a.tma_bytes);
+                    for (int i = 0; i < a.tma_boxes; i++)
+                        tc::tma_load_2d(s + (size_t)i * a.tma_rows * a.vpb, &a.tmap, (int)(2 * v0),
+                                        i * a.tma_rows, &tbar);
+                }
+                const bool got = __syncthreads_and(tc::mbar_wait(&tbar, 0, 1u << 24));
+                if (!got) {
+                    if (tid == 0) atomicExch(a.status, 1);
+                    return;
+                }
+                io.in = nullptr;
+                io.in_es = io.in_vs = 0;
+                io.out = reinterpret_cast<C *>(cout.re) + (cout.off + v0 * cout.vs);
+                io.out_es = cout.es;
+                io.out_vs = cout.vs;
+                io.smask = a.inv ? 0x80000000u : 0u;
+                io.has_scale = a.has_scale != 0;
+                io.scale = a.has_scale ? a.scale : (T)1;
+                io.vf = true;
+                io.mnt = (nt == a.vpb) ? a.mvpb : magic_of((unsigned)nt);
+                // the conjugation of the inverse is folded into the first pass's
+                // input: flip the imaginary parts in place
+                if (a.inv)
+                    for (int i = tid; i < a.tma_boxes * a.tma_rows * a.vpb; i += nthr) s[i].y = -s[i].y;
+                if (a.inv) __syncthreads();
+                staged_tile<T, EMAX>(s, ld, nt, a.vpb, a.passes, a.twg, a.pc, io);
+                return;
+            }
             io.in = reinterpret_cast<const C *>(cin.re) + (cin.off + v0 * cin.vs);
             io.out = reinterpret_cast<C *>(cout.re) + (cout.off + v0 * cout.vs);
             io.in_es = cin.es;

@@ -365,6 +365,10 @@ static VP *create(int type, vsip_length M, vsip_length N, double scale, int dir,
     p->scale = scale;
     p->no_fast = getenv("JVSIP_GPU_NO_FAST") != nullptr;
     p->no_pipeline = getenv("JVSIP_GPU_NO_PIPELINE") != nullptr;
+    {
+        const char *t = getenv("JVSIP_GPU_TMA_COLUMNS");
+        p->tma_columns = t ? (atoi(t) != 0 ? 1 : 0) : -1;
+    }
     p->ntimes = ntimes;
     p->hint = (int)hint;
     p->radix = pass_radices(p->MN, &p->smooth, p->prec == P_F32 ? 1024 : 512);

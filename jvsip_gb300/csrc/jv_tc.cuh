@@ -98,6 +98,21 @@ __device__ __forceinline__ bool mbar_wait(void *mbar, uint32_t phase, uint32_t l
     return false;
 }
 
+// ---- tensor memory access (TMA): the barrier expects `bytes` more bytes of
+// transactions in its current phase (this thread's arrival included)
+__device__ __forceinline__ void mbar_expect_tx(void *mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_addr(mbar)), "r"(bytes)
+                 : "memory");
+}
+// 2-D tiled load of the box at (x, y) of the tensor map into shared memory,
+// completing `bytes` transactions on the barrier (x * element size must be a
+// multiple of 16 bytes)
+__device__ __forceinline__ void tma_load_2d(void *dst, const void *tmap, int x, int y, void *mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        :: "r"(smem_addr(dst)), "l"(tmap), "r"(x), "r"(y), "r"(smem_addr(mbar)) : "memory");
+}
+
 // 32 lanes x 32 bits, 16 consecutive columns per thread
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     uint32_t r[16];

@@ -123,3 +123,41 @@ def test_real_pairs_rows(H, dtype):
         v.destroy()
     for b in (bx, bz, cz, rx):
         b.destroy()
+
+
+@pytest.mark.parametrize("tma", ["auto", "on"])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f", "d"])
+@pytest.mark.parametrize("N,M", [(1000, 4096), (1000, 130), (64, 6), (300, 10), (729, 66), (4096, 34),
+                                 (6174, 18), (16, 8), (17, 12)])
+def test_columns_even_pitch(N, M, dtype, tma, monkeypatch):
+    """Column transforms of an N x M matrix with an even row pitch: the tiles of
+    adjacent columns are staged in shared memory by TMA boxes when the layout
+    allows it (automatically for transforms of 1536 points or more, at every
+    length when JVSIP_GPU_TMA_COLUMNS=1), by the first pass's own loads
+    otherwise; inverse with scale 1/N, and a column count that leaves a
+    partial last tile."""
+    if dtype == np.float64 and N > 8192:
+        pytest.skip("double precision: the shared-memory kernel takes up to 8192 points")
+    if tma == "on":
+        monkeypatch.setenv("JVSIP_GPU_TMA_COLUMNS", "1")
+    else:
+        monkeypatch.delenv("JVSIP_GPU_TMA_COLUMNS", raising=False)
+    z = rng_complex(M * N, N + M, dtype).reshape(N, M)
+    x = interleave(z.reshape(-1), dtype)
+    y = np.zeros_like(x)
+    bx, by = J.CBlock(x), J.CBlock(y)
+    bx.admit(True)
+    by.admit(False)
+    for d, scale in ((J.VSIP_FFT_FWD, 1.0), (J.VSIP_FFT_INV, 1.0 / N)):
+        p = J.FFTM(J.KIND_CCOP, N, M, scale, d, J.VSIP_COL, dtype=dtype)
+        vx, vy = bx.view(0, M, N, 1, M), by.view(0, M, N, 1, M)
+        p.ccfftmop(vx, vy)
+        J.check("columns")
+        by.sync()
+        zz = z.astype(np.complex128)
+        ref = np.fft.fft(zz, axis=0) if d == J.VSIP_FFT_FWD else np.fft.ifft(zz, axis=0)
+        assert rel_l2(deinterleave(y).reshape(N, M), ref) <= tol(N, dtype)
+        vx.destroy()
+        vy.destroy()
+    bx.destroy()
+    by.destroy()
