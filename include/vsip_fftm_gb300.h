@@ -65,6 +65,18 @@ typedef struct vsip_cmviewattributes_f vsip_cmview_f;
 typedef struct vsip_cmviewattributes_d vsip_cmview_d;
 typedef struct vsip_fftmattributes_f   vsip_fftm_f;
 typedef struct vsip_fftmattributes_d   vsip_fftm_d;
+/* c_VSIP_src/vsip.h:174-175, 187-188, 205-206 */
+typedef struct vsip_vviewattributes_f  vsip_vview_f;
+typedef struct vsip_vviewattributes_d  vsip_vview_d;
+typedef struct vsip_cvviewattributes_f vsip_cvview_f;
+typedef struct vsip_cvviewattributes_d vsip_cvview_d;
+typedef struct vsip_fftattributes_f    vsip_fft_f;
+typedef struct vsip_fftattributes_d    vsip_fft_d;
+/* c_VSIP_src/vsip.h:275-276 */
+typedef struct { vsip_scalar_vi input; vsip_scalar_vi output; vsip_fft_place place;
+                 vsip_scalar_d scale; vsip_fft_dir dir; } vsip_fft_attr_d;
+typedef struct { vsip_scalar_vi input; vsip_scalar_vi output; vsip_fft_place place;
+                 vsip_scalar_f scale; vsip_fft_dir dir; } vsip_fft_attr_f;
 /* c_VSIP_src/vsip.h:277-278 */
 typedef struct { vsip_scalar_mi input; vsip_scalar_mi output; vsip_fft_place place;
                  vsip_scalar_d scale; vsip_fft_dir dir; vsip_major major; } vsip_fftm_attr_d;
@@ -131,6 +143,60 @@ void vsip_ccfftmip_d(const vsip_fftm_d *plan, const vsip_cmview_d *xy);
 void vsip_rcfftmop_d(const vsip_fftm_d *plan, const vsip_mview_d *x, const vsip_cmview_d *y);
 /* c_VSIP_src/vsip.h:826 */
 void vsip_crfftmop_d(const vsip_fftm_d *plan, const vsip_cmview_d *x, const vsip_mview_d *y);
+
+/* ======================= single-FFT plans (vectors) ======================= */
+/* A single FFT is the one-row case of the multiple FFT: the same device plan,
+ * kernels, residency rules and error behaviour, with vector views in place of
+ * matrix views.  For rcfftop / crfftop plans N is the real length and the
+ * plan keeps N/2 (c_VSIP_src/VI_rcfftop_create_f_def.h:35). */
+/* c_VSIP_src/vsip.h:1806 -- c_VSIP_src/VI_ccfftop_create_f_def.h:24-81 */
+vsip_fft_f *vsip_ccfftop_create_f(vsip_length N, vsip_scalar_f scale, vsip_fft_dir dir,
+                                  unsigned int ntimes, vsip_alg_hint hint);
+/* c_VSIP_src/vsip.h:1805 */
+vsip_fft_f *vsip_ccfftip_create_f(vsip_length N, vsip_scalar_f scale, vsip_fft_dir dir,
+                                  unsigned int ntimes, vsip_alg_hint hint);
+/* c_VSIP_src/vsip.h:1808 -- c_VSIP_src/VI_rcfftop_create_f_def.h:26-92 */
+vsip_fft_f *vsip_rcfftop_create_f(vsip_length N, vsip_scalar_f scale, unsigned int ntimes,
+                                  vsip_alg_hint hint);
+/* c_VSIP_src/vsip.h:1807 -- c_VSIP_src/VI_crfftop_create_f_def.h:23-89 */
+vsip_fft_f *vsip_crfftop_create_f(vsip_length N, vsip_scalar_f scale, unsigned int ntimes,
+                                  vsip_alg_hint hint);
+/* c_VSIP_src/vsip.h:1802 */
+vsip_fft_d *vsip_ccfftop_create_d(vsip_length N, vsip_scalar_d scale, vsip_fft_dir dir,
+                                  unsigned int ntimes, vsip_alg_hint hint);
+/* c_VSIP_src/vsip.h:1801 */
+vsip_fft_d *vsip_ccfftip_create_d(vsip_length N, vsip_scalar_d scale, vsip_fft_dir dir,
+                                  unsigned int ntimes, vsip_alg_hint hint);
+/* c_VSIP_src/vsip.h:1804 */
+vsip_fft_d *vsip_rcfftop_create_d(vsip_length N, vsip_scalar_d scale, unsigned int ntimes,
+                                  vsip_alg_hint hint);
+/* c_VSIP_src/vsip.h:1803 */
+vsip_fft_d *vsip_crfftop_create_d(vsip_length N, vsip_scalar_d scale, unsigned int ntimes,
+                                  vsip_alg_hint hint);
+/* c_VSIP_src/vsip.h:424 (NULL-safe, returns 0) */
+int vsip_fft_destroy_f(vsip_fft_f *plan);
+/* c_VSIP_src/vsip.h:423 */
+int vsip_fft_destroy_d(vsip_fft_d *plan);
+/* c_VSIP_src/vsip.h:945 -- c_VSIP_src/vsip_fft_getattr_f.c:18-57 */
+void vsip_fft_getattr_f(const vsip_fft_f *plan, vsip_fft_attr_f *attr);
+/* c_VSIP_src/vsip.h:944 */
+void vsip_fft_getattr_d(const vsip_fft_d *plan, vsip_fft_attr_d *attr);
+/* c_VSIP_src/vsip.h:719 -- c_VSIP_src/VI_ccfftop_f_def.h:19-28 (x may alias y) */
+void vsip_ccfftop_f(const vsip_fft_f *plan, const vsip_cvview_f *x, const vsip_cvview_f *y);
+/* c_VSIP_src/vsip.h:713 */
+void vsip_ccfftip_f(const vsip_fft_f *plan, const vsip_cvview_f *xy);
+/* c_VSIP_src/vsip.h:1186 -- c_VSIP_src/VI_rcfftop_f_def.h:22-101 */
+void vsip_rcfftop_f(const vsip_fft_f *plan, const vsip_vview_f *x, const vsip_cvview_f *y);
+/* c_VSIP_src/vsip.h:829 -- c_VSIP_src/VI_crfftop_f_def.h:20-87 */
+void vsip_crfftop_f(const vsip_fft_f *plan, const vsip_cvview_f *x, const vsip_vview_f *y);
+/* c_VSIP_src/vsip.h:718 */
+void vsip_ccfftop_d(const vsip_fft_d *plan, const vsip_cvview_d *x, const vsip_cvview_d *y);
+/* c_VSIP_src/vsip.h:712 */
+void vsip_ccfftip_d(const vsip_fft_d *plan, const vsip_cvview_d *xy);
+/* c_VSIP_src/vsip.h:1185 */
+void vsip_rcfftop_d(const vsip_fft_d *plan, const vsip_vview_d *x, const vsip_cvview_d *y);
+/* c_VSIP_src/vsip.h:828 */
+void vsip_crfftop_d(const vsip_fft_d *plan, const vsip_cvview_d *x, const vsip_vview_d *y);
 
 /* ======================= blocks and views (the fftm boundary) ======================= */
 /* c_VSIP_src/vsip.h:432, 427 -- no-ops in the reference; here they also set up / tear down the device */
@@ -220,6 +286,38 @@ void vsip_cmalldestroy_d(vsip_cmview_d *v);
 void vsip_malldestroy_f(vsip_mview_f *v);
 /* c_VSIP_src/vsip.h:966 */
 void vsip_malldestroy_d(vsip_mview_d *v);
+/* c_VSIP_src/vsip.h:514 -- c_VSIP_src/vsip_cvbind_f.c */
+vsip_cvview_f *vsip_cvbind_f(const vsip_cblock_f *b, vsip_offset o, vsip_stride s, vsip_length n);
+/* c_VSIP_src/vsip.h:517 */
+vsip_cvview_d *vsip_cvbind_d(const vsip_cblock_d *b, vsip_offset o, vsip_stride s, vsip_length n);
+/* c_VSIP_src/vsip.h:491 -- c_VSIP_src/vsip_vbind_f.c */
+vsip_vview_f *vsip_vbind_f(const vsip_block_f *b, vsip_offset o, vsip_stride s, vsip_length n);
+/* c_VSIP_src/vsip.h:503 */
+vsip_vview_d *vsip_vbind_d(const vsip_block_d *b, vsip_offset o, vsip_stride s, vsip_length n);
+/* c_VSIP_src/vsip.h:512 */
+vsip_cvview_f *vsip_cvcreate_f(vsip_length n, vsip_memory_hint h);
+/* c_VSIP_src/vsip.h:515 */
+vsip_cvview_d *vsip_cvcreate_d(vsip_length n, vsip_memory_hint h);
+/* c_VSIP_src/vsip.h:488 */
+vsip_vview_f *vsip_vcreate_f(vsip_length n, vsip_memory_hint h);
+/* c_VSIP_src/vsip.h:501 */
+vsip_vview_d *vsip_vcreate_d(vsip_length n, vsip_memory_hint h);
+/* c_VSIP_src/vsip.h:360 */
+vsip_cblock_f *vsip_cvdestroy_f(vsip_cvview_f *v);
+/* c_VSIP_src/vsip.h:352 */
+vsip_cblock_d *vsip_cvdestroy_d(vsip_cvview_d *v);
+/* c_VSIP_src/vsip.h:304 */
+vsip_block_f *vsip_vdestroy_f(vsip_vview_f *v);
+/* c_VSIP_src/vsip.h:296 */
+vsip_block_d *vsip_vdestroy_d(vsip_vview_d *v);
+/* c_VSIP_src/vsip.h:865 */
+void vsip_cvalldestroy_f(vsip_cvview_f *v);
+/* c_VSIP_src/vsip.h:864 */
+void vsip_cvalldestroy_d(vsip_cvview_d *v);
+/* c_VSIP_src/vsip.h:1292 */
+void vsip_valldestroy_f(vsip_vview_f *v);
+/* c_VSIP_src/vsip.h:1291 */
+void vsip_valldestroy_d(vsip_vview_d *v);
 
 /* ======================= extensions (not VSIPL) ======================= */
 /* Status of the last failed call on this thread (0 = none) and its text;

@@ -1,4 +1,5 @@
-"""jvsip_gb300 -- GB300 (sm_103a) implementation of the VSIPL multiple-FFT calls.
+"""jvsip_gb300 -- GB300 (sm_103a) implementation of the VSIPL multiple-FFT
+calls and of the single-FFT calls built on them.
 
 The product is the C-ABI shared library ``libjvsip_fftm_gb300.so`` (declared
 in ``include/vsip_fftm_gb300.h``).  This package builds it and gives Python
@@ -51,6 +52,15 @@ EXPORTS = [
     "jvsip_gpu_build_info", "jvsip_gpu_synchronize", "jvsip_gpu_stream", "jvsip_fftm_passes", "jvsip_fftm_jofk", "jvsip_fftm_graphs",
     "jvsip_gpu_kernel_launches", "jvsip_ccfftm_noalloc_f", "jvsip_fftm_autotune_f",
     "jvsip_fftm_autotune_entries",
+    "vsip_ccfftop_create_f", "vsip_ccfftip_create_f", "vsip_rcfftop_create_f", "vsip_crfftop_create_f",
+    "vsip_ccfftop_create_d", "vsip_ccfftip_create_d", "vsip_rcfftop_create_d", "vsip_crfftop_create_d",
+    "vsip_fft_destroy_f", "vsip_fft_destroy_d", "vsip_fft_getattr_f", "vsip_fft_getattr_d",
+    "vsip_ccfftop_f", "vsip_ccfftip_f", "vsip_rcfftop_f", "vsip_crfftop_f",
+    "vsip_ccfftop_d", "vsip_ccfftip_d", "vsip_rcfftop_d", "vsip_crfftop_d",
+    "vsip_cvbind_f", "vsip_cvbind_d", "vsip_vbind_f", "vsip_vbind_d",
+    "vsip_cvcreate_f", "vsip_cvcreate_d", "vsip_vcreate_f", "vsip_vcreate_d",
+    "vsip_cvdestroy_f", "vsip_cvdestroy_d", "vsip_vdestroy_f", "vsip_vdestroy_d",
+    "vsip_cvalldestroy_f", "vsip_cvalldestroy_d", "vsip_valldestroy_f", "vsip_valldestroy_d",
 ]
 
 
@@ -66,6 +76,16 @@ class FftmAttrF(C.Structure):
 class FftmAttrD(C.Structure):
     _fields_ = [("input", ScalarMI), ("output", ScalarMI), ("place", C.c_int), ("scale", C.c_double),
                 ("dir", C.c_int), ("major", C.c_int)]
+
+
+class FftAttrF(C.Structure):
+    _fields_ = [("input", C.c_ulong), ("output", C.c_ulong), ("place", C.c_int), ("scale", C.c_float),
+                ("dir", C.c_int)]
+
+
+class FftAttrD(C.Structure):
+    _fields_ = [("input", C.c_ulong), ("output", C.c_ulong), ("place", C.c_int), ("scale", C.c_double),
+                ("dir", C.c_int)]
 
 
 _lib = None
@@ -134,6 +154,33 @@ def lib(load_only: bool = False):
             f.argtypes = [vp]
         getattr(L, "vsip_cmalldestroy" + s).argtypes = [vp]
         getattr(L, "vsip_malldestroy" + s).argtypes = [vp]
+        for name in ("ccfftop_create", "ccfftip_create"):
+            f = getattr(L, "vsip_" + name + s)
+            f.restype = vp
+            f.argtypes = [C.c_ulong, ct, C.c_int, C.c_uint, C.c_int]
+        for name in ("rcfftop_create", "crfftop_create"):
+            f = getattr(L, "vsip_" + name + s)
+            f.restype = vp
+            f.argtypes = [C.c_ulong, ct, C.c_uint, C.c_int]
+        getattr(L, "vsip_fft_destroy" + s).argtypes = [vp]
+        getattr(L, "vsip_fft_getattr" + s).argtypes = [vp, vp]
+        for name, n in (("ccfftop", 3), ("ccfftip", 2), ("rcfftop", 3), ("crfftop", 3)):
+            getattr(L, "vsip_" + name + s).argtypes = [vp] * n
+            getattr(L, "vsip_" + name + s).restype = None
+        for name in ("vsip_cvbind", "vsip_vbind"):
+            f = getattr(L, name + s)
+            f.restype = vp
+            f.argtypes = [vp, C.c_ulong, C.c_long, C.c_ulong]
+        for name in ("vsip_cvcreate", "vsip_vcreate"):
+            f = getattr(L, name + s)
+            f.restype = vp
+            f.argtypes = [C.c_ulong, C.c_int]
+        for name in ("vsip_cvdestroy", "vsip_vdestroy"):
+            f = getattr(L, name + s)
+            f.restype = vp
+            f.argtypes = [vp]
+        getattr(L, "vsip_cvalldestroy" + s).argtypes = [vp]
+        getattr(L, "vsip_valldestroy" + s).argtypes = [vp]
         getattr(L, "jvsip_cblocksync" + s).argtypes = [vp]
         getattr(L, "jvsip_blocksync" + s).argtypes = [vp]
     L.jvsip_gpu_last_error_string.restype = C.c_char_p
@@ -215,6 +262,9 @@ class CBlock:
     def view(self, off, col_stride, col_length, row_stride, row_length):
         return CMView(self, off, col_stride, col_length, row_stride, row_length)
 
+    def vview(self, off, stride, length):
+        return CVView(self, off, stride, length)
+
 
 class RBlock:
     def __init__(self, a: np.ndarray, admit: bool = False, update: bool = True):
@@ -245,6 +295,9 @@ class RBlock:
     def view(self, off, col_stride, col_length, row_stride, row_length):
         return MView(self, off, col_stride, col_length, row_stride, row_length)
 
+    def vview(self, off, stride, length):
+        return VView(self, off, stride, length)
+
 
 class CMView:
     def __init__(self, blk, off, cs, cl, rs, rl):
@@ -265,6 +318,28 @@ class MView:
     def destroy(self):
         if self.h:
             getattr(lib(), "vsip_mdestroy" + self.blk.s)(self.h)
+            self.h = None
+
+
+class CVView:
+    def __init__(self, blk, off, stride, length):
+        self.blk = blk
+        self.h = getattr(lib(), "vsip_cvbind" + blk.s)(blk.h, off, stride, length)
+
+    def destroy(self):
+        if self.h:
+            getattr(lib(), "vsip_cvdestroy" + self.blk.s)(self.h)
+            self.h = None
+
+
+class VView:
+    def __init__(self, blk, off, stride, length):
+        self.blk = blk
+        self.h = getattr(lib(), "vsip_vbind" + blk.s)(blk.h, off, stride, length)
+
+    def destroy(self):
+        if self.h:
+            getattr(lib(), "vsip_vdestroy" + self.blk.s)(self.h)
             self.h = None
 
 
@@ -334,6 +409,62 @@ class FFTM:
     def crfftmop(self, z: CMView, x: MView):
         getattr(lib(), "vsip_crfftmop" + self.s)(self.h, z.h, x.h)
         check("vsip_crfftmop")
+
+
+class FFT:
+    """A vsip_fft_{f,d} single-FFT plan (create / run / getattr / destroy).
+    N is the transform length (the real length for rcfftop / crfftop)."""
+
+    def __init__(self, kind: int, N: int, scale: float = 1.0, dir: int = VSIP_FFT_FWD, dtype=np.float32,
+                 ntimes: int = 0, hint: int = VSIP_ALG_TIME):
+        self.kind, self.s = kind, sfx(dtype)
+        L = lib()
+        if kind in (KIND_CCOP, KIND_CCIP):
+            name = "vsip_ccfftop_create" if kind == KIND_CCOP else "vsip_ccfftip_create"
+            self.h = getattr(L, name + self.s)(N, scale, dir, ntimes, hint)
+        else:
+            name = "vsip_rcfftop_create" if kind == KIND_RCOP else "vsip_crfftop_create"
+            self.h = getattr(L, name + self.s)(N, scale, ntimes, hint)
+        if not self.h:
+            check("plan create")
+            raise RuntimeError("plan create failed")
+
+    def destroy(self):
+        if self.h:
+            getattr(lib(), "vsip_fft_destroy" + self.s)(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    def getattr(self):
+        a = FftAttrF() if self.s == "_f" else FftAttrD()
+        getattr(lib(), "vsip_fft_getattr" + self.s)(self.h, C.byref(a))
+        return a
+
+    def passes(self):
+        buf = (C.c_int * 40)()
+        n = lib().jvsip_fftm_passes(self.h, buf, 40)
+        return list(buf[:n])
+
+    def ccfftop(self, x: CVView, y: CVView):
+        getattr(lib(), "vsip_ccfftop" + self.s)(self.h, x.h, y.h)
+        check("vsip_ccfftop")
+
+    def ccfftip(self, x: CVView):
+        getattr(lib(), "vsip_ccfftip" + self.s)(self.h, x.h)
+        check("vsip_ccfftip")
+
+    def rcfftop(self, x: VView, z: CVView):
+        getattr(lib(), "vsip_rcfftop" + self.s)(self.h, x.h, z.h)
+        check("vsip_rcfftop")
+
+    def crfftop(self, z: CVView, x: VView):
+        getattr(lib(), "vsip_crfftop" + self.s)(self.h, z.h, x.h)
+        check("vsip_crfftop")
 
 
 def gpu_available() -> bool:

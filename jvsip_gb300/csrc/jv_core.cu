@@ -560,6 +560,70 @@ int vsip_finalize(void *ptr) {
 JV_BLOCK_API(f, vsip_scalar_f, vsip_cscalar_f)
 JV_BLOCK_API(d, vsip_scalar_d, vsip_cscalar_d)
 
+// Vector views of the single-FFT calls (c_VSIP_src/vsip_cvbind_f.c,
+// vsip_vbind_f.c, vsip_cvcreate_f.c, vsip_vcreate_f.c, vsip_cvdestroy_f.c,
+// vsip_vdestroy_f.c): the same objects as the reference's.
+#define JV_VECTOR_API(SFX)                                                                           \
+    extern "C" vsip_cvview_##SFX *vsip_cvbind_##SFX(const vsip_cblock_##SFX *b, vsip_offset o,      \
+                                                  vsip_stride s, vsip_length n) {                    \
+        vsip_cvview_##SFX *v = (vsip_cvview_##SFX *)malloc(sizeof(*v));                              \
+        if (!v) return NULL;                                                                         \
+        v->block = (vsip_cblock_##SFX *)b;                                                           \
+        v->offset = o;                                                                               \
+        v->stride = s;                                                                               \
+        v->length = n;                                                                               \
+        v->markings = JV_VALID_OBJECT;                                                               \
+        return v;                                                                                    \
+    }                                                                                                \
+    extern "C" vsip_vview_##SFX *vsip_vbind_##SFX(const vsip_block_##SFX *b, vsip_offset o,         \
+                                                vsip_stride s, vsip_length n) {                      \
+        vsip_vview_##SFX *v = (vsip_vview_##SFX *)malloc(sizeof(*v));                                \
+        if (!v) return NULL;                                                                         \
+        v->block = (vsip_block_##SFX *)b;                                                            \
+        v->offset = o;                                                                               \
+        v->stride = s;                                                                               \
+        v->length = n;                                                                               \
+        v->markings = JV_VALID_OBJECT;                                                               \
+        return v;                                                                                    \
+    }                                                                                                \
+    extern "C" vsip_cvview_##SFX *vsip_cvcreate_##SFX(vsip_length n, vsip_memory_hint h) {          \
+        vsip_cblock_##SFX *b = vsip_cblockcreate_##SFX(n, h);                                        \
+        if (!b) return NULL;                                                                         \
+        vsip_cvview_##SFX *v = vsip_cvbind_##SFX(b, 0, 1, n);                                        \
+        if (!v) vsip_cblockdestroy_##SFX(b);                                                         \
+        return v;                                                                                    \
+    }                                                                                                \
+    extern "C" vsip_vview_##SFX *vsip_vcreate_##SFX(vsip_length n, vsip_memory_hint h) {            \
+        vsip_block_##SFX *b = vsip_blockcreate_##SFX(n, h);                                          \
+        if (!b) return NULL;                                                                         \
+        vsip_vview_##SFX *v = vsip_vbind_##SFX(b, 0, 1, n);                                          \
+        if (!v) vsip_blockdestroy_##SFX(b);                                                          \
+        return v;                                                                                    \
+    }                                                                                                \
+    extern "C" vsip_cblock_##SFX *vsip_cvdestroy_##SFX(vsip_cvview_##SFX *v) {                      \
+        if (!v) return NULL;                                                                         \
+        vsip_cblock_##SFX *b = v->block;                                                             \
+        v->markings = JV_FREED_OBJECT;                                                               \
+        free(v);                                                                                     \
+        return b;                                                                                    \
+    }                                                                                                \
+    extern "C" vsip_block_##SFX *vsip_vdestroy_##SFX(vsip_vview_##SFX *v) {                         \
+        if (!v) return NULL;                                                                         \
+        vsip_block_##SFX *b = v->block;                                                              \
+        v->markings = JV_FREED_OBJECT;                                                               \
+        free(v);                                                                                     \
+        return b;                                                                                    \
+    }                                                                                                \
+    extern "C" void vsip_cvalldestroy_##SFX(vsip_cvview_##SFX *v) {                                 \
+        vsip_cblockdestroy_##SFX(vsip_cvdestroy_##SFX(v));                                           \
+    }                                                                                                \
+    extern "C" void vsip_valldestroy_##SFX(vsip_vview_##SFX *v) {                                   \
+        vsip_blockdestroy_##SFX(vsip_vdestroy_##SFX(v));                                             \
+    }
+
+JV_VECTOR_API(f)
+JV_VECTOR_API(d)
+
 // The library's CUDA stream (as a void*), so callers can order their own work
 // and CUDA events after the fftm calls.
 extern "C" void *jvsip_gpu_stream(void) {

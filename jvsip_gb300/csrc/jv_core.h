@@ -163,10 +163,12 @@ struct Plan {
     void *d_pc = nullptr;     // per-pass constants of that schedule (PassConst, one per pass)
     std::vector<unsigned long> jofk;  // reference digit-reversal map (kept for parity checks)
     std::vector<CallGraph> graphs;    // captured calls (ntimes == 0), most recent last
+    bool single = false;      // a single-FFT plan (vsip_fft_*: one row, vector views)
     std::mutex mu;            // the plan is used by one call at a time
 };
 
 Plan *plan_of(const void *vsip_plan);   // ext_fftm_obj of a vsip_fftm_* (nullptr if bad)
+Plan *plan_of_v(const void *vsip_plan); // ext_fft_obj of a vsip_fft_* (nullptr if bad)
 
 // factorisation of the reference (c_VSIP_src/VI_nuV.h:22-136); returns the stage count
 unsigned long ref_factor(unsigned long N, unsigned long *pn, unsigned long *p0, unsigned long *pF);

@@ -1,4 +1,5 @@
-// jv_exec.cu -- vsip_ccfftmop/ccfftmip/rcfftmop/crfftmop in _f and _d.
+// jv_exec.cu -- vsip_ccfftmop/ccfftmip/rcfftmop/crfftmop in _f and _d, and
+// the single-FFT calls vsip_ccfftop/ccfftip/rcfftop/crfftop on vector views.
 //
 // Semantics follow the reference (c_VSIP_src/VI_ccfftmop_f_def.h:20-29,
 // VI_ccfftmip_f_def.h:17-23, VI_rcfftmop_f_def.h:24-120,
@@ -451,11 +452,10 @@ static bool pipelined_cc(Job &j, const CRes<T, CB> &rx, const CRes<T, CB> &ry, b
     return true;
 }
 
-template <typename T, typename VP, typename CMV, typename CB>
-static void exec_cc(const VP *vp, const CMV *x, const CMV *y, bool ip) {
-    Plan *p = plan_of(vp);
+template <typename T, typename CMV, typename CB>
+static void exec_cc(Plan *p, const CMV *x, const CMV *y, bool ip) {
     if (!p) {
-        set_error(E_ARG, "invalid fftm plan");
+        set_error(E_ARG, "invalid fft plan");
         return;
     }
     if (p->type != JV_CCFFTOP && p->type != JV_CCFFTIP) {
@@ -526,9 +526,8 @@ static void exec_cc(const VP *vp, const CMV *x, const CMV *y, bool ip) {
     if (ok) mark_written(same_view ? (const void *)x->block : (const void *)y->block);
 }
 
-template <typename T, typename VP, typename RMV, typename CMV, typename RB, typename CB>
-static void exec_rc(const VP *vp, const RMV *x, const CMV *z) {
-    Plan *p = plan_of(vp);
+template <typename T, typename RMV, typename CMV, typename RB, typename CB>
+static void exec_rc(Plan *p, const RMV *x, const CMV *z) {
     if (!p || p->type != JV_RCFFTOP) {
         set_error(E_ARG, "invalid real-to-complex fftm plan");
         return;
@@ -562,9 +561,8 @@ static void exec_rc(const VP *vp, const RMV *x, const CMV *z) {
     if (ok) mark_written(z->block);
 }
 
-template <typename T, typename VP, typename CMV, typename RMV, typename CB, typename RB>
-static void exec_cr(const VP *vp, const CMV *z, const RMV *x) {
-    Plan *p = plan_of(vp);
+template <typename T, typename CMV, typename RMV, typename CB, typename RB>
+static void exec_cr(Plan *p, const CMV *z, const RMV *x) {
     if (!p || p->type != JV_CRFFTOP) {
         set_error(E_ARG, "invalid complex-to-real fftm plan");
         return;
@@ -601,6 +599,61 @@ static void exec_cr(const VP *vp, const CMV *z, const RMV *x) {
     }
 }
 
+// A vector view as the one-row matrix view over the same elements (null-safe:
+// a null vector gives a view without a block, which the checks reject).
+static vsip_cmview_f row_of(const vsip_cvview_f *v) {
+    vsip_cmview_f m;
+    memset(&m, 0, sizeof(m));
+    if (!v) return m;
+    m.block = v->block;
+    m.offset = v->offset;
+    m.row_stride = v->stride;
+    m.row_length = v->length;
+    m.col_stride = (vsip_stride)v->length * v->stride;
+    m.col_length = 1;
+    m.markings = v->markings;
+    return m;
+}
+static vsip_cmview_d row_of(const vsip_cvview_d *v) {
+    vsip_cmview_d m;
+    memset(&m, 0, sizeof(m));
+    if (!v) return m;
+    m.block = v->block;
+    m.offset = v->offset;
+    m.row_stride = v->stride;
+    m.row_length = v->length;
+    m.col_stride = (vsip_stride)v->length * v->stride;
+    m.col_length = 1;
+    m.markings = v->markings;
+    return m;
+}
+static vsip_mview_f row_of(const vsip_vview_f *v) {
+    vsip_mview_f m;
+    memset(&m, 0, sizeof(m));
+    if (!v) return m;
+    m.block = v->block;
+    m.offset = v->offset;
+    m.row_stride = v->stride;
+    m.row_length = v->length;
+    m.col_stride = (vsip_stride)v->length * v->stride;
+    m.col_length = 1;
+    m.markings = v->markings;
+    return m;
+}
+static vsip_mview_d row_of(const vsip_vview_d *v) {
+    vsip_mview_d m;
+    memset(&m, 0, sizeof(m));
+    if (!v) return m;
+    m.block = v->block;
+    m.offset = v->offset;
+    m.row_stride = v->stride;
+    m.row_length = v->length;
+    m.col_stride = (vsip_stride)v->length * v->stride;
+    m.col_length = 1;
+    m.markings = v->markings;
+    return m;
+}
+
 }  // namespace jv
 
 using namespace jv;
@@ -608,28 +661,73 @@ using namespace jv;
 extern "C" {
 
 void vsip_ccfftmop_f(const vsip_fftm_f *p, const vsip_cmview_f *x, const vsip_cmview_f *y) {
-    exec_cc<float, vsip_fftm_f, vsip_cmview_f, vsip_cblock_f>(p, x, y, false);
+    exec_cc<float, vsip_cmview_f, vsip_cblock_f>(plan_of(p), x, y, false);
 }
 void vsip_ccfftmip_f(const vsip_fftm_f *p, const vsip_cmview_f *xy) {
-    exec_cc<float, vsip_fftm_f, vsip_cmview_f, vsip_cblock_f>(p, xy, xy, true);
+    exec_cc<float, vsip_cmview_f, vsip_cblock_f>(plan_of(p), xy, xy, true);
 }
 void vsip_ccfftmop_d(const vsip_fftm_d *p, const vsip_cmview_d *x, const vsip_cmview_d *y) {
-    exec_cc<double, vsip_fftm_d, vsip_cmview_d, vsip_cblock_d>(p, x, y, false);
+    exec_cc<double, vsip_cmview_d, vsip_cblock_d>(plan_of(p), x, y, false);
 }
 void vsip_ccfftmip_d(const vsip_fftm_d *p, const vsip_cmview_d *xy) {
-    exec_cc<double, vsip_fftm_d, vsip_cmview_d, vsip_cblock_d>(p, xy, xy, true);
+    exec_cc<double, vsip_cmview_d, vsip_cblock_d>(plan_of(p), xy, xy, true);
 }
 void vsip_rcfftmop_f(const vsip_fftm_f *p, const vsip_mview_f *x, const vsip_cmview_f *z) {
-    exec_rc<float, vsip_fftm_f, vsip_mview_f, vsip_cmview_f, vsip_block_f, vsip_cblock_f>(p, x, z);
+    exec_rc<float, vsip_mview_f, vsip_cmview_f, vsip_block_f, vsip_cblock_f>(plan_of(p), x, z);
 }
 void vsip_rcfftmop_d(const vsip_fftm_d *p, const vsip_mview_d *x, const vsip_cmview_d *z) {
-    exec_rc<double, vsip_fftm_d, vsip_mview_d, vsip_cmview_d, vsip_block_d, vsip_cblock_d>(p, x, z);
+    exec_rc<double, vsip_mview_d, vsip_cmview_d, vsip_block_d, vsip_cblock_d>(plan_of(p), x, z);
 }
 void vsip_crfftmop_f(const vsip_fftm_f *p, const vsip_cmview_f *z, const vsip_mview_f *x) {
-    exec_cr<float, vsip_fftm_f, vsip_cmview_f, vsip_mview_f, vsip_cblock_f, vsip_block_f>(p, z, x);
+    exec_cr<float, vsip_cmview_f, vsip_mview_f, vsip_cblock_f, vsip_block_f>(plan_of(p), z, x);
 }
 void vsip_crfftmop_d(const vsip_fftm_d *p, const vsip_cmview_d *z, const vsip_mview_d *x) {
-    exec_cr<double, vsip_fftm_d, vsip_cmview_d, vsip_mview_d, vsip_cblock_d, vsip_block_d>(p, z, x);
+    exec_cr<double, vsip_cmview_d, vsip_mview_d, vsip_cblock_d, vsip_block_d>(plan_of(p), z, x);
+}
+
+// Single FFTs (c_VSIP_src/VI_ccfftop_f_def.h:19-28, VI_ccfftip_f.h,
+// VI_rcfftop_f_def.h:22-101, VI_crfftop_f_def.h:20-87): a vector view of
+// `length` elements `stride` apart is the one-row matrix view with that row
+// stride, so the single FFT runs the multiple-FFT path with one transform.
+void vsip_ccfftop_f(const vsip_fft_f *p, const vsip_cvview_f *x, const vsip_cvview_f *y) {
+    vsip_cmview_f mx = row_of(x), my = row_of(y);
+    exec_cc<float, vsip_cmview_f, vsip_cblock_f>(plan_of_v(p), x ? &mx : nullptr, y ? &my : nullptr, false);
+}
+void vsip_ccfftip_f(const vsip_fft_f *p, const vsip_cvview_f *xy) {
+    vsip_cmview_f m = row_of(xy);
+    exec_cc<float, vsip_cmview_f, vsip_cblock_f>(plan_of_v(p), xy ? &m : nullptr, xy ? &m : nullptr, true);
+}
+void vsip_ccfftop_d(const vsip_fft_d *p, const vsip_cvview_d *x, const vsip_cvview_d *y) {
+    vsip_cmview_d mx = row_of(x), my = row_of(y);
+    exec_cc<double, vsip_cmview_d, vsip_cblock_d>(plan_of_v(p), x ? &mx : nullptr, y ? &my : nullptr, false);
+}
+void vsip_ccfftip_d(const vsip_fft_d *p, const vsip_cvview_d *xy) {
+    vsip_cmview_d m = row_of(xy);
+    exec_cc<double, vsip_cmview_d, vsip_cblock_d>(plan_of_v(p), xy ? &m : nullptr, xy ? &m : nullptr, true);
+}
+void vsip_rcfftop_f(const vsip_fft_f *p, const vsip_vview_f *x, const vsip_cvview_f *z) {
+    vsip_mview_f mx = row_of(x);
+    vsip_cmview_f mz = row_of(z);
+    exec_rc<float, vsip_mview_f, vsip_cmview_f, vsip_block_f, vsip_cblock_f>(plan_of_v(p), x ? &mx : nullptr,
+                                                                            z ? &mz : nullptr);
+}
+void vsip_rcfftop_d(const vsip_fft_d *p, const vsip_vview_d *x, const vsip_cvview_d *z) {
+    vsip_mview_d mx = row_of(x);
+    vsip_cmview_d mz = row_of(z);
+    exec_rc<double, vsip_mview_d, vsip_cmview_d, vsip_block_d, vsip_cblock_d>(plan_of_v(p), x ? &mx : nullptr,
+                                                                             z ? &mz : nullptr);
+}
+void vsip_crfftop_f(const vsip_fft_f *p, const vsip_cvview_f *z, const vsip_vview_f *x) {
+    vsip_cmview_f mz = row_of(z);
+    vsip_mview_f mx = row_of(x);
+    exec_cr<float, vsip_cmview_f, vsip_mview_f, vsip_cblock_f, vsip_block_f>(plan_of_v(p), z ? &mz : nullptr,
+                                                                            x ? &mx : nullptr);
+}
+void vsip_crfftop_d(const vsip_fft_d *p, const vsip_cvview_d *z, const vsip_vview_d *x) {
+    vsip_cmview_d mz = row_of(z);
+    vsip_mview_d mx = row_of(x);
+    exec_cr<double, vsip_cmview_d, vsip_mview_d, vsip_cblock_d, vsip_block_d>(plan_of_v(p), z ? &mz : nullptr,
+                                                                             x ? &mx : nullptr);
 }
 
 const char *jvsip_gpu_build_info(void) {

@@ -1,5 +1,7 @@
 // jv_plan.cu -- multiple-FFT plans: vsip_{cc,rc,cr}fftm{op,ip}_create_{f,d},
-// vsip_fftm_destroy_{f,d}, vsip_fftm_getattr_{f,d}.
+// vsip_fftm_destroy_{f,d}, vsip_fftm_getattr_{f,d}; single-FFT plans:
+// vsip_{cc,rc,cr}fft{op,ip}_create_{f,d}, vsip_fft_destroy_{f,d},
+// vsip_fft_getattr_{f,d}.
 //
 // A plan is the reference's plan object (layout of
 // c_VSIP_src/vsip_fftmattributes_f.h:8-38, attributes filled with the
@@ -17,6 +19,7 @@
 #include <map>
 #include <mutex>
 #include <new>
+#include <set>
 #include <tuple>
 
 #include "jv_core.h"
@@ -330,23 +333,39 @@ Plan *plan_of(const void *vp) {
     if (!vp) return nullptr;
     // both precisions share the layout up to ext_fftm_obj
     const vsip_fftm_f *f = (const vsip_fftm_f *)vp;
-    return (Plan *)f->ext_fftm_obj;
+    Plan *p = (Plan *)f->ext_fftm_obj;
+    return (p && !p->single) ? p : nullptr;
 }
 
-template <typename VP, typename T>
-static VP *create(int type, vsip_length M, vsip_length N, double scale, int dir, vsip_major major,
-                  unsigned ntimes, vsip_alg_hint hint) {
-    if (!device()) return NULL;
-    VP *vp = (VP *)calloc(1, sizeof(VP));
-    if (!vp) {
-        set_error(E_ALLOC, "plan allocation");
-        return NULL;
-    }
+// Addresses of the live single-FFT plan objects, so the introspection calls
+// that take either kind of plan (as const void *) can tell them apart.
+static std::mutex g_single_mu;
+static std::set<const void *> g_single;
+
+static bool is_single(const void *vp) {
+    std::lock_guard<std::mutex> lk(g_single_mu);
+    return g_single.count(vp) != 0;
+}
+
+Plan *plan_of_v(const void *vp) {
+    if (!vp) return nullptr;
+    // both precisions share the layout up to ext_fft_obj
+    const vsip_fft_f *f = (const vsip_fft_f *)vp;
+    Plan *p = (Plan *)f->ext_fft_obj;
+    return (p && p->single) ? p : nullptr;
+}
+
+// The device plan of M x N transforms (a single FFT is M = 1, VSIP_ROW);
+// *ns and *dft receive the reference's factor count and DFT flag.  Returns
+// nullptr (error recorded, nothing left allocated) on failure.
+template <typename T>
+static Plan *new_plan(int type, vsip_length M, vsip_length N, double scale, int dir, vsip_major major,
+                      unsigned ntimes, vsip_alg_hint hint, unsigned long *ns_out, int *dft_out) {
+    if (!device()) return nullptr;
     Plan *p = new (std::nothrow) Plan();
     if (!p) {
-        free(vp);
         set_error(E_ALLOC, "plan allocation");
-        return NULL;
+        return nullptr;
     }
     p->type = type;
     p->prec = sizeof(T) == 4 ? P_F32 : P_F64;
@@ -385,6 +404,26 @@ static VP *create(int type, vsip_length M, vsip_length N, double scale, int dir,
         dfree(p->d_twg);
         dfree(p->d_pc);
         delete p;
+        return nullptr;
+    }
+    *ns_out = ns;
+    *dft_out = (ns > 0 && p0[0] == 1 && pF[0] == (unsigned long)p->MN) ? 1 : 0;
+    return p;
+}
+
+template <typename VP, typename T>
+static VP *create(int type, vsip_length M, vsip_length N, double scale, int dir, vsip_major major,
+                  unsigned ntimes, vsip_alg_hint hint) {
+    if (!device()) return NULL;
+    VP *vp = (VP *)calloc(1, sizeof(VP));
+    if (!vp) {
+        set_error(E_ALLOC, "plan allocation");
+        return NULL;
+    }
+    unsigned long ns = 0;
+    int dft = 0;
+    Plan *p = new_plan<T>(type, M, N, scale, dir, major, ntimes, hint, &ns, &dft);
+    if (!p) {
         free(vp);
         return NULL;
     }
@@ -398,11 +437,48 @@ static VP *create(int type, vsip_length M, vsip_length N, double scale, int dir,
     vp->length = ns;
     vp->d = (vsip_fft_dir)p->dir;
     vp->type = type;
-    vp->dft = (ns > 0 && p0[0] == 1 && pF[0] == (unsigned long)p->MN) ? 1 : 0;
+    vp->dft = dft;
     vp->ntimes = ntimes;
     vp->hint = hint;
     vp->ext_fftm_obj = p;
     return vp;
+}
+
+// A single-FFT plan (c_VSIP_src/vsip_fftattributes_f.h:8-31): the device plan
+// of one row of N points.  fft->N is the transform length, the half length for
+// rcfftop / crfftop (c_VSIP_src/VI_rcfftop_create_f_def.h:35,
+// VI_crfftop_create_f_def.h:32); the reference's work arrays are not needed.
+template <typename FP, typename T>
+static FP *create_v(int type, vsip_length N, double scale, int dir, unsigned ntimes, vsip_alg_hint hint) {
+    if (!device()) return NULL;
+    FP *fp = (FP *)calloc(1, sizeof(FP));
+    if (!fp) {
+        set_error(E_ALLOC, "plan allocation");
+        return NULL;
+    }
+    unsigned long ns = 0;
+    int dft = 0;
+    Plan *p = new_plan<T>(type, 1, N, scale, dir, VSIP_ROW, ntimes, hint, &ns, &dft);
+    if (!p) {
+        free(fp);
+        return NULL;
+    }
+    p->single = true;
+    fp->scale = (T)scale;
+    fp->N = (vsip_length)p->MN;
+    fp->length = ns;
+    fp->d = (vsip_fft_dir)p->dir;
+    fp->type = type;
+    fp->dft = dft;
+    fp->ntimes = ntimes;
+    fp->hint = hint;
+    fp->stage = 0;
+    fp->ext_fft_obj = p;
+    {
+        std::lock_guard<std::mutex> lk(g_single_mu);
+        g_single.insert(fp);
+    }
+    return fp;
 }
 
 template <typename VP>
@@ -412,6 +488,43 @@ static int destroy(VP *vp) {
         free(vp);
     }
     return 0;
+}
+
+template <typename FP>
+static int destroy_v(FP *fp) {
+    if (fp) {
+        {
+            std::lock_guard<std::mutex> lk(g_single_mu);
+            g_single.erase(fp);
+        }
+        plan_free((Plan *)fp->ext_fft_obj);
+        free(fp);
+    }
+    return 0;
+}
+
+template <typename FP, typename A>
+static void getattr_v(const FP *fft, A *attr) {
+    // c_VSIP_src/vsip_fft_getattr_f.c:18-57: lengths of the input and output
+    // vectors (real lengths 2N for rcfftop / crfftop, N + 1 for the half spectrum)
+    if (!fft || !attr) return;
+    attr->input = fft->N;
+    attr->output = fft->N;
+    attr->place = VSIP_FFT_OP;
+    switch (fft->type) {
+        case JV_CCFFTIP: attr->place = VSIP_FFT_IP; break;
+        case JV_RCFFTOP:
+            attr->input = fft->N * 2;
+            attr->output = fft->N + 1;
+            break;
+        case JV_CRFFTOP:
+            attr->input = fft->N + 1;
+            attr->output = fft->N * 2;
+            break;
+        default: break;
+    }
+    attr->dir = fft->d;
+    attr->scale = fft->scale;
 }
 
 template <typename VP, typename A>
@@ -479,6 +592,39 @@ vsip_fftm_d *vsip_crfftmop_create_d(vsip_length M, vsip_length N, vsip_scalar_d 
     return create<vsip_fftm_d, double>(JV_CRFFTOP, M, N, scale, VSIP_FFT_INV, major, ntimes, hint);
 }
 
+vsip_fft_f *vsip_ccfftop_create_f(vsip_length N, vsip_scalar_f scale, vsip_fft_dir dir, unsigned int ntimes,
+                                  vsip_alg_hint hint) {
+    return create_v<vsip_fft_f, float>(JV_CCFFTOP, N, scale, dir, ntimes, hint);
+}
+vsip_fft_f *vsip_ccfftip_create_f(vsip_length N, vsip_scalar_f scale, vsip_fft_dir dir, unsigned int ntimes,
+                                  vsip_alg_hint hint) {
+    return create_v<vsip_fft_f, float>(JV_CCFFTIP, N, scale, dir, ntimes, hint);
+}
+vsip_fft_f *vsip_rcfftop_create_f(vsip_length N, vsip_scalar_f scale, unsigned int ntimes, vsip_alg_hint hint) {
+    return create_v<vsip_fft_f, float>(JV_RCFFTOP, N, scale, VSIP_FFT_FWD, ntimes, hint);
+}
+vsip_fft_f *vsip_crfftop_create_f(vsip_length N, vsip_scalar_f scale, unsigned int ntimes, vsip_alg_hint hint) {
+    return create_v<vsip_fft_f, float>(JV_CRFFTOP, N, scale, VSIP_FFT_INV, ntimes, hint);
+}
+vsip_fft_d *vsip_ccfftop_create_d(vsip_length N, vsip_scalar_d scale, vsip_fft_dir dir, unsigned int ntimes,
+                                  vsip_alg_hint hint) {
+    return create_v<vsip_fft_d, double>(JV_CCFFTOP, N, scale, dir, ntimes, hint);
+}
+vsip_fft_d *vsip_ccfftip_create_d(vsip_length N, vsip_scalar_d scale, vsip_fft_dir dir, unsigned int ntimes,
+                                  vsip_alg_hint hint) {
+    return create_v<vsip_fft_d, double>(JV_CCFFTIP, N, scale, dir, ntimes, hint);
+}
+vsip_fft_d *vsip_rcfftop_create_d(vsip_length N, vsip_scalar_d scale, unsigned int ntimes, vsip_alg_hint hint) {
+    return create_v<vsip_fft_d, double>(JV_RCFFTOP, N, scale, VSIP_FFT_FWD, ntimes, hint);
+}
+vsip_fft_d *vsip_crfftop_create_d(vsip_length N, vsip_scalar_d scale, unsigned int ntimes, vsip_alg_hint hint) {
+    return create_v<vsip_fft_d, double>(JV_CRFFTOP, N, scale, VSIP_FFT_INV, ntimes, hint);
+}
+int vsip_fft_destroy_f(vsip_fft_f *p) { return destroy_v(p); }
+int vsip_fft_destroy_d(vsip_fft_d *p) { return destroy_v(p); }
+void vsip_fft_getattr_f(const vsip_fft_f *p, vsip_fft_attr_f *a) { getattr_v(p, a); }
+void vsip_fft_getattr_d(const vsip_fft_d *p, vsip_fft_attr_d *a) { getattr_v(p, a); }
+
 int vsip_fftm_destroy_f(vsip_fftm_f *p) { return destroy(p); }
 int vsip_fftm_destroy_d(vsip_fftm_d *p) { return destroy(p); }
 void vsip_fftm_getattr_f(const vsip_fftm_f *p, vsip_fftm_attr_f *a) { getattr(p, a); }
@@ -497,15 +643,17 @@ int jvsip_fftm_getform_f(const vsip_fftm_f *vp) {
 
 // Plan introspection for tests and tools: the device pass radices and the
 // reference digit-reversal map.  Returns the count written (or needed).
+static Plan *any_plan(const void *vp) { return is_single(vp) ? plan_of_v(vp) : plan_of(vp); }
+
 int jvsip_fftm_passes(const void *vp, int *radix, int cap) {
-    Plan *p = plan_of(vp);
+    Plan *p = any_plan(vp);
     if (!p) return -1;
     int n = (int)p->radix.size();
     for (int i = 0; i < n && i < cap; i++) radix[i] = p->radix[i];
     return n;
 }
 int jvsip_fftm_graphs(const void *vp) {
-    Plan *p = plan_of(vp);
+    Plan *p = any_plan(vp);
     if (!p) return -1;
     std::lock_guard<std::mutex> lk(p->mu);
     int n = 0;
@@ -513,7 +661,7 @@ int jvsip_fftm_graphs(const void *vp) {
     return n;
 }
 long jvsip_fftm_jofk(const void *vp, unsigned long *out, long cap) {
-    Plan *p = plan_of(vp);
+    Plan *p = any_plan(vp);
     if (!p) return -1;
     long n = (long)p->jofk.size();
     for (long i = 0; i < n && i < cap; i++) out[i] = p->jofk[i];

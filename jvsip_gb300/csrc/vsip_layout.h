@@ -10,6 +10,9 @@
  *   real view     c_VSIP_src/vsip_mviewattributes_f.h:47-55
  *   complex view  c_VSIP_src/vsip_cmviewattributes_f.h:47-55
  *   plan          c_VSIP_src/vsip_fftmattributes_f.h:8-38
+ *   vector views  c_VSIP_src/vsip_vviewattributes_f.h:46-52,
+ *                 c_VSIP_src/vsip_cvviewattributes_f.h:45-51
+ *   vector plan   c_VSIP_src/vsip_fftattributes_f.h:6-31
  *   constants     c_VSIP_src/VI.h:5-13
  *
  * The plan struct is opaque to callers; its first part mirrors the reference
@@ -108,5 +111,40 @@ enum { JV_CCFFTOP = 0, JV_CCFFTIP = 1, JV_RCFFTOP = 2, JV_CRFFTOP = 3 };
 
 JV_LAYOUT_PLAN(f, vsip_scalar_f)
 JV_LAYOUT_PLAN(d, vsip_scalar_d)
+
+/* Vector views and the vector FFT plan (single transforms: one-row fftm). */
+#define JV_LAYOUT_VECTOR(SFX, T)                                                         \
+    struct vsip_vviewattributes_##SFX {                                                   \
+        vsip_block_##SFX *block;                                                          \
+        vsip_offset offset;                                                               \
+        vsip_stride stride;                                                               \
+        vsip_length length;                                                               \
+        int markings;                                                                     \
+    };                                                                                    \
+    struct vsip_cvviewattributes_##SFX {                                                  \
+        vsip_cblock_##SFX *block;                                                         \
+        vsip_offset offset;                                                               \
+        vsip_stride stride;                                                               \
+        vsip_length length;                                                               \
+        int markings;                                                                     \
+    };                                                                                    \
+    struct vsip_fftattributes_##SFX {                                                     \
+        void *wt, *temp, *bit, *index, *pn, *p0, *pF, *x;                                 \
+        T *x_r, *x_i, *xp_r, *xp_i;                                                       \
+        vsip_stride xst, xpst;                                                            \
+        T scale;                                                                          \
+        vsip_length N;      /* length (R2C / C2R: the half length) */                     \
+        vsip_length length; /* number of factor stages             */                     \
+        vsip_fft_dir d;                                                                   \
+        int type;                                                                         \
+        int dft;                                                                          \
+        unsigned int ntimes;                                                              \
+        vsip_alg_hint hint;                                                               \
+        vsip_scalar_vi stage;                                                             \
+        void *ext_fft_obj;  /* -> struct jv_plan (device plan) */                         \
+    };
+
+JV_LAYOUT_VECTOR(f, vsip_scalar_f)
+JV_LAYOUT_VECTOR(d, vsip_scalar_d)
 
 #endif

@@ -79,6 +79,27 @@ def lib():
             f = getattr(L, "vsip_mdestroy" + s)
             f.restype = C.c_void_p
             f.argtypes = [C.c_void_p]
+            # single-FFT plans and vector views
+            for name in ("ccfftop_create", "ccfftip_create"):
+                f = getattr(L, "vsip_" + name + s)
+                f.restype = C.c_void_p
+                f.argtypes = [C.c_ulong, ct, C.c_int, C.c_uint, C.c_int]
+            for name in ("rcfftop_create", "crfftop_create"):
+                f = getattr(L, "vsip_" + name + s)
+                f.restype = C.c_void_p
+                f.argtypes = [C.c_ulong, ct, C.c_uint, C.c_int]
+            getattr(L, "vsip_fft_destroy" + s).argtypes = [C.c_void_p]
+            getattr(L, "vsip_fft_getattr" + s).argtypes = [C.c_void_p, C.c_void_p]
+            for name, n in (("ccfftop", 3), ("ccfftip", 2), ("rcfftop", 3), ("crfftop", 3)):
+                getattr(L, "vsip_" + name + s).argtypes = [C.c_void_p] * n
+            for name in ("vsip_cvbind", "vsip_vbind"):
+                f = getattr(L, name + s)
+                f.restype = C.c_void_p
+                f.argtypes = [C.c_void_p, C.c_ulong, C.c_long, C.c_ulong]
+            for name in ("vsip_cvdestroy", "vsip_vdestroy"):
+                f = getattr(L, name + s)
+                f.restype = C.c_void_p
+                f.argtypes = [C.c_void_p]
         L.vsip_init(None)
     return _lib
 
@@ -86,14 +107,16 @@ def lib():
 class _Bound:
     """A user block bound to a view's numpy storage, admitted for the call."""
 
-    def __init__(self, v, real: bool):
+    def __init__(self, v, real: bool, with_view: bool = True):
         L, s = lib(), sfx(v.buf.dtype)
         self.L, self.s, self.real = L, s, real
+        self.view = None
         if real:
             self.blk = getattr(L, "vsip_blockbind" + s)(v.buf.ctypes.data, v.buf.size, 0)
             getattr(L, "vsip_blockadmit" + s)(self.blk, 1)
-            self.view = getattr(L, "vsip_mbind" + s)(self.blk, v.off, v.col_stride, v.col_length,
-                                                     v.row_stride, v.row_length)
+            if with_view:
+                self.view = getattr(L, "vsip_mbind" + s)(self.blk, v.off, v.col_stride, v.col_length,
+                                                         v.row_stride, v.row_length)
         else:
             if v.split:
                 self.blk = getattr(L, "vsip_cblockbind" + s)(v.buf.ctypes.data, v.im.ctypes.data,
@@ -102,17 +125,20 @@ class _Bound:
                 self.blk = getattr(L, "vsip_cblockbind" + s)(v.buf.ctypes.data, None,
                                                              v.buf.size // 2, 0)
             getattr(L, "vsip_cblockadmit" + s)(self.blk, 1)
-            self.view = getattr(L, "vsip_cmbind" + s)(self.blk, v.off, v.col_stride, v.col_length,
-                                                      v.row_stride, v.row_length)
+            if with_view:
+                self.view = getattr(L, "vsip_cmbind" + s)(self.blk, v.off, v.col_stride, v.col_length,
+                                                          v.row_stride, v.row_length)
 
     def close(self):
         L, s = self.L, self.s
         if self.real:
-            getattr(L, "vsip_mdestroy" + s)(self.view)
+            if self.view:
+                getattr(L, "vsip_mdestroy" + s)(self.view)
             getattr(L, "vsip_blockrelease" + s)(self.blk, 1)
             getattr(L, "vsip_blockdestroy" + s)(self.blk)
         else:
-            getattr(L, "vsip_cmdestroy" + s)(self.view)
+            if self.view:
+                getattr(L, "vsip_cmdestroy" + s)(self.view)
             a, b = C.c_void_p(), C.c_void_p()
             getattr(L, "vsip_cblockrelease" + s)(self.blk, 1, C.byref(a), C.byref(b))
             getattr(L, "vsip_cblockdestroy" + s)(self.blk)
@@ -172,3 +198,59 @@ class RefPlan:
 
     def crfftmop(self, z: CView, x: RView):
         self._run("crfftmop", (z, False), (x, True))
+
+
+class RefFFT:
+    """A reference single-FFT plan (vsip_{cc,rc,cr}fft{op,ip}_create_*) run on
+    one-row views: a view with col_length 1 is bound as the vector of its
+    row_length elements row_stride apart.  Views whose buffers are the same
+    numpy array are bound on one block (x and y in one block)."""
+
+    def __init__(self, kind, N, scale=1.0, dir=-1, dtype=np.float32):
+        L = lib()
+        self.s = sfx(dtype)
+        self.kind = kind
+        if kind in (CCOP, CCIP):
+            name = "ccfftop_create" if kind == CCOP else "ccfftip_create"
+            self.h = getattr(L, "vsip_" + name + self.s)(N, scale, dir, 0, 0)
+        else:
+            name = "rcfftop_create" if kind == RCOP else "crfftop_create"
+            self.h = getattr(L, "vsip_" + name + self.s)(N, scale, 0, 0)
+        if not self.h:
+            raise MemoryError("reference plan creation failed")
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            getattr(lib(), "vsip_fft_destroy" + self.s)(h)
+            self.h = None
+
+    def _run(self, name, *views):
+        L, s = lib(), self.s
+        blocks = {}
+        vecs = []
+        for v, real in views:
+            assert v.col_length == 1
+            key = id(v.buf)
+            if key not in blocks:
+                blocks[key] = _Bound(v, real, with_view=False)
+            b = blocks[key]
+            vecs.append(getattr(L, ("vsip_vbind" if real else "vsip_cvbind") + s)(b.blk, v.off, v.row_stride,
+                                                                                 v.row_length))
+        getattr(L, "vsip_" + name + s)(self.h, *vecs)
+        for (v, real), h in zip(views, vecs):
+            getattr(L, ("vsip_vdestroy" if real else "vsip_cvdestroy") + s)(h)
+        for b in blocks.values():
+            b.close()
+
+    def ccfftop(self, x, y):
+        self._run("ccfftop", (x, False), (y, False))
+
+    def ccfftip(self, y):
+        self._run("ccfftip", (y, False))
+
+    def rcfftop(self, x, z):
+        self._run("rcfftop", (x, True), (z, False))
+
+    def crfftop(self, z, x):
+        self._run("crfftop", (z, False), (x, True))

@@ -1,7 +1,9 @@
 """Loading and materialising the golden fixtures of tests/golden/.
 
 A case describes one VSIPL fftm call (kind, precision, plan arguments and the
-input/output views).  `build_case` recreates its blocks from the stored seeds
+input/output views), or -- with "single" set -- one single-FFT call on
+vectors, stored as a one-row view (col_length 1, the vector's stride as
+row_stride); "shared" puts y in x's block.  `build_case` recreates its blocks from the stored seeds
 (or the stored inputs); `check_output` compares an output block with the
 reference's, whole or through the stored sample.
 """
@@ -18,6 +20,8 @@ import pyoracle as O
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 _meta = None
 _arrays = None
+_fft_meta = None
+_fft_arrays = None
 
 
 def meta():
@@ -37,6 +41,34 @@ def arrays():
 
 def cases():
     return meta()["cases"]
+
+
+def fft_meta():
+    global _fft_meta
+    if _fft_meta is None:
+        with open(os.path.join(GOLDEN, "fft_cases.json")) as f:
+            _fft_meta = json.load(f)
+    return _fft_meta
+
+
+def fft_arrays():
+    global _fft_arrays
+    if _fft_arrays is None:
+        _fft_arrays = dict(np.load(os.path.join(GOLDEN, "fft_cases.npz")))
+    return _fft_arrays
+
+
+def fft_cases():
+    return fft_meta()["cases"]
+
+
+def fft_kats():
+    with open(os.path.join(GOLDEN, "fft_kat.json")) as f:
+        return json.load(f)
+
+
+def arrays_of(case):
+    return fft_arrays() if case.get("single") else arrays()
 
 
 def ref_tests():
@@ -90,26 +122,30 @@ def build_case(case):
     """Return (x_view, y_view_or_None) with the case's input data in place."""
     dtype = dtype_of(case)
     kind = case["kind"]
+    A = arrays_of(case)
     if kind in ("ccop", "ccip"):
         x = make_cview(case["x"], dtype)
         if case.get("stored_input"):
-            _load_input(x, arrays()[case["id"] + "__in"])
+            _load_input(x, A[case["id"] + "__in"])
         if kind == "ccip" or case.get("alias"):
             return x, None
+        if case.get("shared"):
+            ys = case["y"]
+            return x, O.CView(x.buf, ys["off"], ys["cs"], ys["cl"], ys["rs"], ys["rl"], x.im)
         return x, make_cview(case["y"], dtype)
     if kind == "rcop":
         x = make_rview(case["x"], dtype)
         if case.get("stored_input"):
-            x.buf[:] = arrays()[case["id"] + "__in"]
+            x.buf[:] = A[case["id"] + "__in"]
         return x, make_cview(case["y"], dtype)
     z = make_cview(case["x"], dtype)
     if case.get("stored_input"):
-        _load_input(z, arrays()[case["id"] + "__in"])
+        _load_input(z, A[case["id"] + "__in"])
     return z, make_rview(case["y"], dtype)
 
 
 def output_block(case, x, y):
-    if case["kind"] == "ccip" or case.get("alias"):
+    if case["kind"] == "ccip" or case.get("alias") or case.get("shared"):
         return block_arrays(x)
     return block_arrays(y)
 
@@ -120,7 +156,7 @@ def sha256(a: np.ndarray) -> str:
 
 def reference_values(case):
     """(indices, values) of the reference output block available in the fixture."""
-    A = arrays()
+    A = arrays_of(case)
     if case["stored_output"]:
         v = A[case["id"] + "__out"]
         return np.arange(v.size), v
@@ -140,3 +176,60 @@ def rel_l2(a: np.ndarray, b: np.ndarray) -> float:
     den = np.sqrt(np.sum(b * b))
     num = np.sqrt(np.sum((a - b) ** 2))
     return float(num / den) if den > 0 else float(num)
+
+
+# ------------------------------------------------------------------ single-FFT known-answer tests
+def cplx(pairs) -> np.ndarray:
+    a = np.asarray(pairs, np.float64).reshape(-1, 2)
+    return a[:, 0] + 1j * a[:, 1]
+
+
+def kat_views(t):
+    """(x view, y view or None) of a single-FFT known-answer test with its
+    input in place: dense vectors in blocks of `block` elements, or -- for
+    ccfftop_sc -- x and y bound on one block at (offset, stride) xbind / ybind."""
+    dtype = np.float32 if t["prec"] == "f" else np.float64
+    n, kind = t["n"], t["kind"]
+    xin = t["x"] if isinstance(t["x"], np.ndarray) else cplx(t["x"])
+    if kind == "rcop":
+        x = O.RView(np.zeros(t["block"], dtype), 0, n, 1, 1, n)
+        x.set(np.asarray(xin).real[None, :])
+        z = O.CView(np.zeros(2 * t["block"], dtype), 0, n // 2 + 1, 1, 1, n // 2 + 1)
+        return x, z
+    if kind == "crop":
+        z = O.CView(np.zeros(2 * t["block"], dtype), 0, n // 2 + 1, 1, 1, n // 2 + 1)
+        z.set(np.asarray(xin)[None, :])
+        y = O.RView(np.zeros(t["block"], dtype), 0, n, 1, 1, n)
+        return z, y
+    if t.get("shared"):
+        buf = np.zeros(2 * t["block"], dtype)
+        xo, xs = t["xbind"]
+        yo, ys = t["ybind"]
+        x = O.CView(buf, xo, n * xs, 1, xs, n)
+        y = O.CView(buf, yo, n * ys, 1, ys, n)
+        x.set(np.asarray(xin)[None, :])
+        return x, y
+    x = O.CView(np.zeros(2 * t["block"], dtype), 0, n, 1, 1, n)
+    x.set(np.asarray(xin)[None, :])
+    if kind == "ccip":
+        return x, None
+    return x, O.CView(np.zeros(2 * t["block"], dtype), 0, n, 1, 1, n)
+
+
+def kat_run(t, plan):
+    """Run a known-answer test through `plan`, any object with the single-FFT
+    methods ccfftop / ccfftip / rcfftop / crfftop taking one-row views;
+    returns the output vector (complex128)."""
+    x, y = kat_views(t)
+    k = t["kind"]
+    if k == "ccop":
+        plan.ccfftop(x, y)
+        return y.get()[0]
+    if k == "ccip":
+        plan.ccfftip(x)
+        return x.get()[0]
+    if k == "rcop":
+        plan.rcfftop(x, y)
+        return y.get()[0]
+    plan.crfftop(x, y)
+    return y.get()[0].astype(np.complex128)

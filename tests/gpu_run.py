@@ -10,13 +10,16 @@ import pyoracle as O
 KIND = dict(ccop=J.KIND_CCOP, ccip=J.KIND_CCIP, rcop=J.KIND_RCOP, crop=J.KIND_CROP)
 
 
-def _bind(v, admit):
-    if isinstance(v, O.CView):
-        b = J.CBlock(v.buf, v.im)
-        view = b.view(v.off, v.col_stride, v.col_length, v.row_stride, v.row_length)
-    else:
-        b = J.RBlock(v.buf)
-        view = b.view(v.off, v.col_stride, v.col_length, v.row_stride, v.row_length)
+def _view(b, v, single):
+    if single:
+        # a one-row view stands for the vector of its row
+        return b.vview(v.off, v.row_stride, v.row_length)
+    return b.view(v.off, v.col_stride, v.col_length, v.row_stride, v.row_length)
+
+
+def _bind(v, admit, single=False):
+    b = J.CBlock(v.buf, v.im) if isinstance(v, O.CView) else J.RBlock(v.buf)
+    view = _view(b, v, single)
     if admit:
         b.admit(True)
     return b, view
@@ -26,13 +29,31 @@ def run_case_gpu(case, admit: bool):
     """Run a golden case through the library; returns (out_block, in_block_before)."""
     x, y = G.build_case(case)
     before = G.output_block(case, x, y).copy()
-    bx, vx = _bind(x, admit)
-    by, vy = (bx, vx) if y is None else _bind(y, admit)
-    p = J.FFTM(KIND[case["kind"]], case["M"], case["N"], case["scale"], case["dir"], case["major"],
-               G.dtype_of(case))
+    single = bool(case.get("single"))
+    bx, vx = _bind(x, admit, single)
+    if y is None:
+        by, vy = bx, vx
+    elif case.get("shared"):
+        by, vy = bx, _view(bx, y, single)
+    else:
+        by, vy = _bind(y, admit, single)
+    if single:
+        p = J.FFT(KIND[case["kind"]], case["N"], case["scale"], case["dir"], G.dtype_of(case))
+    else:
+        p = J.FFTM(KIND[case["kind"]], case["M"], case["N"], case["scale"], case["dir"], case["major"],
+                   G.dtype_of(case))
     try:
         k = case["kind"]
-        if k == "ccop":
+        if single:
+            if k == "ccop":
+                p.ccfftop(vx, vx if case.get("alias") else vy)
+            elif k == "ccip":
+                p.ccfftip(vx)
+            elif k == "rcop":
+                p.rcfftop(vx, vy)
+            else:
+                p.crfftop(vx, vy)
+        elif k == "ccop":
             p.ccfftmop(vx, vx if case.get("alias") else vy)
         elif k == "ccip":
             p.ccfftmip(vx)
@@ -63,6 +84,8 @@ def view_mask(case):
         m[v.index()] = True
         return m
     v = G.make_cview(out_spec, dtype)
+    if case.get("shared"):
+        v = G.make_cview(dict(case["x"]) | {k: out_spec[k] for k in ("off", "cs", "cl", "rs", "rl")}, dtype)
     idx = v.index()
     if v.split:
         m = np.zeros(2 * v.buf.size, bool)

@@ -54,12 +54,23 @@ int main(void) {
          O(vsip_mviewattributes_d, markings));
   printf("%lu %lu %lu %lu\n", (unsigned long)sizeof(struct vsip_fftmattributes_f),
          O(vsip_fftmattributes_f, scale), O(vsip_fftmattributes_f, MN), O(vsip_fftmattributes_f, ext_fftm_obj));
+  printf("%lu %lu %lu %lu %lu %lu\n", (unsigned long)sizeof(struct vsip_vviewattributes_f),
+         O(vsip_vviewattributes_f, length), O(vsip_vviewattributes_f, markings),
+         (unsigned long)sizeof(struct vsip_cvviewattributes_d), O(vsip_cvviewattributes_d, stride),
+         O(vsip_cvviewattributes_d, markings));
+  printf("%lu %lu %lu %lu %lu %lu\n", (unsigned long)sizeof(struct vsip_fftattributes_f),
+         O(vsip_fftattributes_f, scale), O(vsip_fftattributes_f, N), O(vsip_fftattributes_f, ext_fft_obj),
+         (unsigned long)sizeof(struct vsip_fftattributes_d), O(vsip_fftattributes_d, ext_fft_obj));
+  printf("%lu %lu\n", (unsigned long)sizeof(vsip_fft_attr_f), (unsigned long)sizeof(vsip_fft_attr_d));
   return 0; }
 '''
 # sizes and offsets of the reference's default build on LP64 hosts
 # (c_VSIP_src/vsip_cblockattributes_f.h:42-67, vsip_blockattributes_f.h:40-51,
-#  vsip_cmviewattributes_f.h:47-55, vsip_fftmattributes_f.h:8-38)
-LAYOUT_REF = ["88 24 52 84 128 120 56 52", "56 40 56 48", "256 160 184 248"]
+#  vsip_cmviewattributes_f.h:47-55, vsip_fftmattributes_f.h:8-38,
+#  vsip_vviewattributes_f.h:46-52, vsip_cvviewattributes_d.h, vsip_fftattributes_f.h:8-31,
+#  vsip.h:275-276)
+LAYOUT_REF = ["88 24 52 84 128 120 56 52", "56 40 56 48", "256 160 184 248", "40 24 32 40 16 32",
+              "176 112 120 168 176 168", "32 40"]
 
 
 def test_object_layouts_match_the_reference(tmp_path):
@@ -67,7 +78,7 @@ def test_object_layouts_match_the_reference(tmp_path):
     src.write_text(LAYOUT_PROBE)
     exe = tmp_path / "layout"
     subprocess.check_call(["gcc", "-std=c99", "-I", ROOT, str(src), "-o", str(exe)])
-    out = subprocess.check_output([str(exe)], text=True).split("\n")[:3]
+    out = subprocess.check_output([str(exe)], text=True).split("\n")[:6]
     assert out == LAYOUT_REF
 
 
@@ -80,6 +91,10 @@ def test_no_gpu_create_returns_null_with_error():
     code, msg = J.last_error()
     assert code == 1 and "device" in msg
     assert L.vsip_fftm_destroy_f(None) == 0
+    assert L.vsip_ccfftop_create_f(1024, 1.0, -1, 0, 0) is None
+    assert L.vsip_rcfftop_create_d(1024, 1.0, 0, 0) is None
+    assert L.vsip_fft_destroy_f(None) == 0
+    assert L.vsip_fft_destroy_d(None) == 0
 
 
 def test_block_lifecycle_without_gpu():
@@ -91,4 +106,7 @@ def test_block_lifecycle_without_gpu():
     v = L.vsip_cmbind_f(b, 0, 4, 4, 1, 4)
     assert v
     assert L.vsip_cmdestroy_f(v) == b
+    w = L.vsip_cvbind_f(b, 2, -1, 3)
+    assert w
+    assert L.vsip_cvdestroy_f(w) == b
     L.vsip_cblockdestroy_f(b)

@@ -1,6 +1,9 @@
-"""The CPU oracle against the reference: every golden case bit for bit, and
-the reference's own known-answer tests (c_VSIP_testing/ccfftm{op,ip}_{f,d}.h)
-at their own acceptance level (mean square error < 2e-4)."""
+"""The CPU oracle against the reference: every golden case bit for bit (the
+multiple-FFT cases, and the single-FFT cases run as one-row fftm calls), the
+reference's own fftm known-answer tests (c_VSIP_testing/ccfftm{op,ip}_{f,d}.h)
+at their own acceptance level (mean square error < 2e-4), and its single-FFT
+known-answer tests (c_VSIP_testing/ccfftop_f.h and the rest) at theirs
+(|y - expected| <= 0.001 elementwise)."""
 import numpy as np
 import pytest
 
@@ -31,7 +34,7 @@ def test_generator_is_stable():
     assert float(np.sum(probe * np.arange(4096))) == G.meta()["generator_probe_sum"]
 
 
-@pytest.mark.parametrize("case", G.cases(), ids=lambda c: c["id"])
+@pytest.mark.parametrize("case", G.cases() + G.fft_cases(), ids=lambda c: c["id"])
 def test_oracle_matches_reference_bit_for_bit(case):
     out = run_oracle(case)
     assert out.size == case["out_size"]
@@ -58,6 +61,33 @@ def test_oracle_passes_reference_known_answer_tests(tc):
         got = x.get()
     meansq = float(np.mean(np.abs(got - gold) ** 2))
     assert meansq < tc["tol_meansq"]
+
+
+class OracleFFT:
+    """The oracle as a single-FFT plan: the fftm restatement with one row."""
+
+    def __init__(self, t):
+        dtype = np.float32 if t["prec"] == "f" else np.float64
+        self.p = O.Plan(KIND[t["kind"]], 1, t["n"], t["scale"], t["dir"], O.ROW, dtype)
+
+    def ccfftop(self, x, y):
+        self.p.ccfftmop(x, y)
+
+    def ccfftip(self, x):
+        self.p.ccfftmip(x)
+
+    def rcfftop(self, x, z):
+        self.p.rcfftmop(x, z)
+
+    def crfftop(self, z, x):
+        self.p.crfftmop(z, x)
+
+
+@pytest.mark.parametrize("t", G.fft_kats(), ids=lambda t: f"{t['file'].split('/')[-1]}:n{t['n']}")
+def test_oracle_passes_reference_single_fft_tests(t):
+    got = G.kat_run(t, OracleFFT(t))
+    assert float(np.max(np.abs(got - G.cplx(t["expect"])))) <= 1e-3
+    assert np.array_equal(got, G.cplx(t["ref_out"])) == t["oracle_bit_exact"]
 
 
 def test_factorisation_and_digit_reversal():
