@@ -25,7 +25,8 @@ Other configurations (--workload): cfg1 (64x1024), cfg2col (1000-point
 columns x 4096), cfg2rc / cfg2cr (4096 x 1536 real <-> 4096 x 769), cfg3d
 (16384 x 4096 c128), cfg4 (32768 x 1024, rows scaled by 10^U(-3,3)), cfg5
 (batching: uneven lengths and row counts in one launch vs a loop of per-plan
-calls), measured the same way.
+calls), vec / vecd / vecrc (one single FFT of --points points: c64, c128,
+real f32 -> c64), measured the same way.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload NAME]
 
@@ -49,7 +50,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "batched FFT GB/s (% HBM peak): split-TC & batched vs plain FP32 at ≤1e-6 rel err"
 FALLBACK_HBM = 6800.0
-WORKLOADS = ["cfg3", "cfg1", "cfg2col", "cfg2rc", "cfg2cr", "cfg3d", "cfg4", "cfg5"]
+WORKLOADS = ["cfg3", "cfg1", "cfg2col", "cfg2rc", "cfg2cr", "cfg3d", "cfg4", "cfg5", "vec", "vecd", "vecrc"]
 
 
 def args():
@@ -68,6 +69,7 @@ def args():
     ap.add_argument("--no-autotune", action="store_true",
                     help="cfg5: use the cached or heuristic tiling (profiling runs: no tuner launches)")
     ap.add_argument("--batch-gb", type=float, default=2.0, help="cfg5: bytes per buffer of the instance sequence (0: the literal 20000 instances)")
+    ap.add_argument("--points", type=int, default=1 << 24, help="vec / vecd / vecrc: single-FFT length")
     return ap.parse_args()
 
 
@@ -334,6 +336,29 @@ def other_workload(a):
             call = lambda: L.vsip_crfftmop_f(plan.h, vx.h, vy.h)
             desc = "vsip_crfftmop_f 4096x769 c64 -> 4096x1536 f32 VSIP_ROW, scale 1/1536"
         nbytes, dt = M * (4 * N + 8 * H), "f32"
+    elif w in ("vec", "vecd", "vecrc"):
+        # one single FFT of --points points (vsip_ccfftop / vsip_rcfftop)
+        N = M = a.points
+        if w == "vecrc":
+            x = synth.fill(N, 8, 1)
+            y = np.zeros(2 * (N // 2 + 1), np.float32)
+            plan = J.FFT(J.KIND_RCOP, N, 1.0)
+            bx, by = J.RBlock(x), J.CBlock(y)
+            vx, vy = bx.vview(0, 1, N), by.vview(0, 1, N // 2 + 1)
+            call = lambda: L.vsip_rcfftop_f(plan.h, vx.h, vy.h)
+            nbytes, dt = 4 * N + 8 * (N // 2 + 1), "f32"
+            desc = f"vsip_rcfftop_f {N} f32 -> {N // 2 + 1} c64, N(0,1)"
+        else:
+            dtype = np.float32 if w == "vec" else np.float64
+            x = synth.fill(2 * N, 7, 1, dtype)
+            y = np.zeros_like(x)
+            plan = J.FFT(J.KIND_CCOP, N, 1.0, -1, dtype)
+            bx, by = J.CBlock(x), J.CBlock(y)
+            vx, vy = bx.vview(0, 1, N), by.vview(0, 1, N)
+            fn = L.vsip_ccfftop_f if w == "vec" else L.vsip_ccfftop_d
+            call = lambda: fn(plan.h, vx.h, vy.h)
+            nbytes, dt = (16 if w == "vec" else 32) * N, ("f32" if w == "vec" else "f64")
+            desc = f"vsip_ccfftop_{'f' if w == 'vec' else 'd'} {N} points {'c64' if w == 'vec' else 'c128'} forward, N(0,1)"
     else:  # cfg3d
         M, N = 16384, 4096
         g = torch.Generator(device="cuda").manual_seed(4)

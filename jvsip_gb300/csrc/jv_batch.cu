@@ -62,11 +62,12 @@ __device__ __forceinline__ void batch_tile(const TileDesc &d, float2 *s) {
     io.in_vs = d.in_vs;
     io.out_es = d.out_es;
     io.out_vs = d.out_vs;
-    io.smask = d.inv ? 0x80000000u : 0u;
+    io.smask_in = io.smask_out = d.inv ? 0x80000000u : 0u;
     io.has_scale = d.has_scale != 0;
     io.scale = d.has_scale ? d.scale : 1.f;
-    io.vf = d.vec_fast != 0;
+    io.vf = io.vf_out = d.vec_fast != 0;
     io.mnt = d.mnt;
+    io.tw_lo = io.tw_hi = nullptr;
     c2c_tile<float, BEMAX>(s, d.ld, d.nt, d.passes, d.twg, d.pc, io);
 }
 

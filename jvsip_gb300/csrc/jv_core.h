@@ -110,6 +110,14 @@ struct Job {
     bool no_pipeline = false;  // JVSIP_GPU_NO_PIPELINE at plan creation: one staging copy each way
     int tma_columns = -1;      // JVSIP_GPU_TMA_COLUMNS at plan creation: 1 / 0 force TMA-staged
                                // column tiles on / off, -1 (unset) automatic
+    // the steps of a long transform (shared-memory kernel, interleaved c2c only)
+    int conj_in = -1, conj_out = -1;   // conjugate on load / store: -1 follows inv
+    long nbatch = 1;                   // groups of nvec transforms along the grid's y
+    long bvs_in = 0, bvs_out = 0;      // complex-element offset between groups
+    const void *tw_lo = nullptr;       // output twiddle W^(g*k) of the first step, g = t*tw_ts +
+    const void *tw_hi = nullptr;       //   group*tw_ys: tw_lo[m & tw_mask] * tw_hi[m >> tw_sh]
+    unsigned tw_mask = 0, tw_sh = 0, tw_ts = 0, tw_ys = 0;
+    struct LongPlan *lp = nullptr;     // the plan's long-transform decomposition (or null)
 };
 
 // A device-resident call of a plan captured into a CUDA graph: plans created
@@ -122,6 +130,21 @@ struct CallGraph {
     bool failed = false;            // capture was refused: run directly
 };
 void count_launch_undo(unsigned long long n);  // launches recorded by a capture did not run
+
+// A transform of N = N1 * N2 points too long for one CTA, as two steps of the
+// shared-memory kernel: A, N1 transforms of N2 points down the columns of x
+// seen as an N2 x N1 row-major matrix (x[n1 + N1*n2]), each output element k2
+// multiplied by W_N^(n1*k2) and stored as row n1 of an N1 x N2 scratch
+// matrix; B, N2 transforms of N1 points down the scratch's columns, element
+// k1 of column k2 stored at y[k2 + N2*k1].
+struct LongPlan {
+    long N1 = 0, N2 = 0;
+    struct Plan *p1 = nullptr, *p2 = nullptr;  // c2c plans of N1 and N2 points (schedules, tables)
+    void *d_lo = nullptr, *d_hi = nullptr;     // two-level table of W_N^m: lo[m & mask] * hi[m >> sh]
+    unsigned mask = 0, sh = 0;
+    void *scratch = nullptr;                   // nvec * N complex, allocated at the first call
+    size_t scratch_bytes = 0;
+};
 
 // Kernel entry points (defined in the kernel translation units).
 bool launch_smem_f32(const Job &j, cudaStream_t s);
@@ -164,6 +187,7 @@ struct Plan {
     std::vector<unsigned long> jofk;  // reference digit-reversal map (kept for parity checks)
     std::vector<CallGraph> graphs;    // captured calls (ntimes == 0), most recent last
     bool single = false;      // a single-FFT plan (vsip_fft_*: one row, vector views)
+    LongPlan *lp = nullptr;   // two-step decomposition when MN is too long for one CTA
     std::mutex mu;            // the plan is used by one call at a time
 };
 

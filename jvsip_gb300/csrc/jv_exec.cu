@@ -257,6 +257,123 @@ static bool job_in_smem(const Job &j) {
     return smooth && need <= lim;
 }
 
+// The two steps of a long c2c transform (LongPlan): interleaved views only;
+// returns false with *handled unset when the views do not qualify.
+static bool interleaved(const CView &v, size_t esz) {
+    return v.cst == 2 && (const char *)v.im == (const char *)v.re + esz && ((uintptr_t)v.re % (2 * esz)) == 0;
+}
+
+static bool step_job(Job &q, const Job &j, const Plan *sp) {
+    q.kind = K_C2C;
+    q.prec = j.prec;
+    q.N = sp->MN;
+    q.tw = sp->d_tw;
+    q.twg = sp->d_twg;
+    q.pc = sp->d_pc;
+    q.twp = nullptr;
+    q.thalf = nullptr;
+    q.form = 0;
+    q.no_fast = true;
+    q.tma_columns = j.tma_columns;
+    q.npass = (int)sp->radix.size();
+    if (q.npass > 40) return false;
+    for (int i = 0; i < q.npass; i++) q.radix[i] = sp->radix[i];
+    q.inplace = 0;
+    q.lp = nullptr;
+    return true;
+}
+
+static bool run_long(Job &j, cudaStream_t st, bool *handled) {
+    *handled = false;
+    LongPlan *lp = j.lp;
+    const size_t esz = j.prec == P_F32 ? sizeof(float) : sizeof(double);
+    if (!lp || j.kind != K_C2C || !interleaved(j.cin, esz) || !interleaved(j.cout, esz)) return false;
+    const long N = j.N, N1 = lp->N1, N2 = lp->N2, nv = j.nvec;
+    const size_t need = (size_t)nv * N * 2 * esz;
+    *handled = true;
+    if (lp->scratch_bytes < need) {
+        // held by the plan (a captured call replays into it)
+        dfree(lp->scratch);
+        lp->scratch = dmalloc(need);
+        lp->scratch_bytes = lp->scratch ? need : 0;
+        if (!lp->scratch) {
+            if (!jvsip_gpu_last_error()) set_error(E_ALLOC, "scratch of a long transform");
+            return false;
+        }
+    }
+    char *sc = (char *)lp->scratch;
+    CView scv;
+    scv.re = sc;
+    scv.im = sc + esz;
+    scv.cst = 2;
+    scv.off = 0;
+    // transforms of a vector far apart in memory ("rows": |vs| != 1 or one
+    // vector): groups are the vectors, transforms inside a group are n1 (step
+    // A) / k2 (step B).  Adjacent vectors ("columns", |vs| == 1): groups are
+    // n1 / k2 and the transforms inside a group are the vectors, adjacent in
+    // memory; the scratch then holds [n1][k2][v].
+    const bool cols = nv > 1 && (j.cin.vs == 1 || j.cin.vs == -1);
+    Job a = j, b = j;
+    if (!step_job(a, j, lp->p2) || !step_job(b, j, lp->p1)) return false;
+    // step A: transform over n2 (N2 points, element n1 + N1*n2 of x)
+    a.cin = j.cin;
+    a.cout = scv;
+    a.conj_in = j.inv;
+    a.conj_out = 0;
+    a.has_scale = 0;
+    a.scale = 1.0;
+    a.tw_lo = lp->d_lo;
+    a.tw_hi = lp->d_hi;
+    a.tw_mask = lp->mask;
+    a.tw_sh = lp->sh;
+    // step B: transform over n1 (N1 points) of the scratch, k1 to y[k2 + N2*k1]
+    b.cin = scv;
+    b.cout = j.cout;
+    b.conj_in = 0;
+    b.conj_out = j.inv;
+    if (!cols) {
+        a.nvec = N1;
+        a.nbatch = nv;
+        a.cin.es = j.cin.es * N1;
+        a.cin.vs = j.cin.es;
+        a.bvs_in = j.cin.vs;
+        a.cout.es = 1;
+        a.cout.vs = N2;
+        a.bvs_out = N;
+        a.tw_ts = 1;
+        a.tw_ys = 0;
+        b.nvec = N2;
+        b.nbatch = nv;
+        b.cin.es = N2;
+        b.cin.vs = 1;
+        b.bvs_in = N;
+        b.cout.es = j.cout.es * N2;
+        b.cout.vs = j.cout.es;
+        b.bvs_out = j.cout.vs;
+    } else {
+        a.nvec = nv;
+        a.nbatch = N1;
+        a.cin.es = j.cin.es * N1;
+        a.cin.vs = j.cin.vs;
+        a.bvs_in = j.cin.es;
+        a.cout.es = nv;
+        a.cout.vs = 1;
+        a.bvs_out = N2 * nv;
+        a.tw_ts = 0;
+        a.tw_ys = 1;
+        b.nvec = nv;
+        b.nbatch = N2;
+        b.cin.es = N2 * nv;
+        b.cin.vs = 1;
+        b.bvs_in = nv;
+        b.cout.es = j.cout.es * N2;
+        b.cout.vs = j.cout.vs;
+        b.bvs_out = j.cout.es;
+    }
+    if (j.prec == P_F32) return launch_smem_f32(a, st) && launch_smem_f32(b, st);
+    return launch_smem_f64(a, st) && launch_smem_f64(b, st);
+}
+
 static bool run_job(Job &j, cudaStream_t st) {
     if (j.nvec <= 0 || j.N <= 0) return true;
     if (j.form == JVSIP_FORM_SPLIT_BF16 || j.form == JVSIP_FORM_SPLIT_FP16) {
@@ -268,6 +385,11 @@ static bool run_job(Job &j, cudaStream_t st) {
             return launch_smem_f32(j, st);
         }
         return launch_smem_f64(j, st);
+    }
+    if (j.lp) {
+        bool handled = false;
+        const bool ok = run_long(j, st, &handled);
+        if (handled) return ok;
     }
     return j.prec == P_F32 ? launch_global_f32(j, st) : launch_global_f64(j, st);
 }
@@ -295,7 +417,12 @@ static constexpr size_t kPlanGraphs = 8;
 static bool run_job_planned(Plan *p, Job &j, cudaStream_t st) {
     if (p->ntimes != 0 || j.nvec <= 0 || j.N <= 0) return run_job(j, st);
     const bool split = (j.form == JVSIP_FORM_SPLIT_BF16 || j.form == JVSIP_FORM_SPLIT_FP16);
-    if (!split && !job_in_smem(j)) return run_job(j, st);
+    // a long transform captures once its plan holds the scratch for this call
+    const size_t esz = j.prec == P_F32 ? sizeof(float) : sizeof(double);
+    const bool long_ready = j.lp && j.kind == K_C2C && interleaved(j.cin, esz) && interleaved(j.cout, esz) &&
+                            j.lp->scratch_bytes >= (size_t)j.nvec * j.N * 2 * esz;
+    const bool long_job = j.lp && j.kind == K_C2C && interleaved(j.cin, esz) && interleaved(j.cout, esz);
+    if (!split && !job_in_smem(j) && !long_job) return run_job(j, st);
     CallGraph *e = nullptr;
     for (CallGraph &g : p->graphs)
         if (same_call(g.key, j)) e = &g;
@@ -309,7 +436,7 @@ static bool run_job_planned(Plan *p, Job &j, cudaStream_t st) {
         p->graphs.push_back(g);
         return run_job(j, st);
     }
-    if (!e->exec && !e->failed) {
+    if (!e->exec && !e->failed && (!long_job || long_ready)) {
         cudaStream_t cs = nullptr;
         cudaGraph_t graph = nullptr;
         const int err0 = jvsip_gpu_last_error();
@@ -346,6 +473,8 @@ static bool run_job_planned(Plan *p, Job &j, cudaStream_t st) {
 // current when the call returns.  All-resident calls return asynchronously;
 // work on the library stream is ordered, and release / sync wait for it.
 static bool finish(Staging &stg, cudaStream_t st, bool ok) {
+    // a failed step that did not say why still leaves a status for the caller
+    if (!ok && !jvsip_gpu_last_error()) set_error(E_UNSUPPORTED, "fft execution path refused the call");
     if (stg.regs.empty()) return ok;
     ok = ok && stg.download(st);
     return cuda_ok(cudaStreamSynchronize(st), "fftm execution") && ok;
@@ -370,6 +499,7 @@ static void fill_job(Job &j, const Plan *p, int kind) {
     j.tma_columns = p->tma_columns;
     j.npass = (int)p->radix.size();
     for (int i = 0; i < j.npass && i < 40; i++) j.radix[i] = p->radix[i];
+    j.lp = p->lp;
 }
 
 // Host-resident c2c call whose views are rows of unit element stride and

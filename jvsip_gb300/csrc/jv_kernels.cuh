@@ -419,6 +419,21 @@ template <typename T> struct SmemArgs {
     int tma, tma_boxes, tma_rows;
     unsigned tma_bytes;
     int *status;      // set to 1 when the bounded wait for the boxes expired
+    // c2c tiles of column-type views: ld_rows / st_rows load / store with
+    // consecutive threads on consecutive elements of one transform (the view
+    // side that is row-contiguous), the other side with consecutive threads on
+    // adjacent transforms
+    int ld_rows, st_rows;
+    int conj_in, conj_out;  // conjugate on load / on store (both = inv for a whole transform)
+    // batch of vector groups along gridDim.y: group y starts bvs_in / bvs_out
+    // complex elements after group 0 (the steps of a long transform)
+    long bvs_in, bvs_out;
+    // output twiddle of the first step of a long transform: output element k
+    // of transform t in group y is multiplied by W^(g*k), g = t*tw_ts +
+    // (y0 + y)*tw_ys, as tw_lo[m & tw_mask] * tw_hi[m >> tw_sh], m = g*k
+    const typename cplx_t<T>::t *tw_lo, *tw_hi;
+    unsigned tw_mask, tw_sh, tw_ts, tw_ys;
+    long y0;          // group index of this launch's first group
     CUtensorMap tmap;
     WalkConst win, wout;  // load / store walker constants for full tiles of vpb transforms
     CAcc<T> cin;
@@ -540,12 +555,23 @@ template <typename T> struct TileIO {
     const C *in;     // interleaved input; element (t, n) at in[t*in_vs + n*in_es]
     C *out;          // interleaved output; element (t, n) at out[t*out_vs + n*out_es]
     long in_es, in_vs, out_es, out_vs;
-    unsigned smask;  // 0x80000000: inverse (conjugate on load and on store), else 0
+    unsigned smask_in, smask_out;  // 0x80000000: conjugate on load / on store, else 0
     bool has_scale;
     T scale;         // 1 when the plan has no scale
-    bool vf;         // t-fastest mapping
+    bool vf;         // t-fastest mapping of the loads
+    bool vf_out;     // t-fastest mapping of the stores
     unsigned mnt;    // multiply-high magic of the tile's transform count
+    // output twiddle W^(g*k), g = tw_t0 + t*tw_ts (none when tw_lo is null)
+    const C *tw_lo, *tw_hi;
+    unsigned tw_mask, tw_sh, tw_t0, tw_ts;
 };
+
+// W^m from the two-level table of a long transform's output twiddles
+template <typename C>
+__device__ __forceinline__ C tw_two_level(const C *__restrict__ lo, const C *__restrict__ hi, unsigned mask,
+                                          unsigned sh, unsigned m) {
+    return cmul(__ldg(&lo[m & mask]), __ldg(&hi[m >> sh]));
+}
 
 __device__ __forceinline__ void tile_tj(int b, bool vf, int nt, unsigned mnt, int NR, unsigned mNR, int &t, int &j) {
     if (vf) {
@@ -578,7 +604,7 @@ __device__ __forceinline__ void pass_first(typename cplx_t<T>::t *s, int ld, int
 #pragma unroll
             for (int r = 0; r < R; r++) {
                 C c = src[r * st];
-                c.y = flip_sign(c.y, io.smask);
+                c.y = flip_sign(c.y, io.smask_in);
                 v[k][r] = c;
             }
         }
@@ -594,7 +620,8 @@ __device__ __forceinline__ void pass_first(typename cplx_t<T>::t *s, int ld, int
                 // one pass: N = R, j = 0, output element r
                 C *dst = io.out + (long)t * io.out_vs;
 #pragma unroll
-                for (int r = 0; r < R; r++) dst[r * io.out_es] = out_value(v[k][r], io.smask, io.has_scale, io.scale);
+                for (int r = 0; r < R; r++)
+                    dst[r * io.out_es] = out_value(v[k][r], io.smask_out, io.has_scale, io.scale);
             } else {
                 C *dst = s + t * ld;
 #pragma unroll
@@ -620,7 +647,7 @@ __device__ __forceinline__ void pass_last(const typename cplx_t<T>::t *s, int ld
         const int b = tid + k * nthr;
         if (b < nb) {
             int t, j;
-            tile_tj(b, io.vf, nt, io.mnt, NR, pc.y, t, j);
+            tile_tj(b, io.vf_out, nt, io.mnt, NR, pc.y, t, j);
             const C *src = s + t * ld;
 #pragma unroll
             for (int r = 0; r < R; r++) v[k][r] = src[spad(j + r * NR)];
@@ -631,16 +658,24 @@ __device__ __forceinline__ void pass_last(const typename cplx_t<T>::t *s, int ld
         const int b = tid + k * nthr;
         if (b < nb) {
             int t, j;
-            tile_tj(b, io.vf, nt, io.mnt, NR, pc.y, t, j);
+            tile_tj(b, io.vf_out, nt, io.mnt, NR, pc.y, t, j);
             if (j) {
 #pragma unroll
                 for (int r = 1; r < R; r++) v[k][r] = cmul(v[k][r], __ldg(&tp[r * Ns + j]));
             }
             Dft<C, R>::run(v[k]);
+            if (io.tw_lo) {
+                // output element j + r*Ns of transform t: times W^(g*(j + r*Ns))
+                const unsigned tg = io.tw_t0 + (unsigned)t * io.tw_ts;
+#pragma unroll
+                for (int r = 0; r < R; r++)
+                    v[k][r] = cmul(v[k][r], tw_two_level(io.tw_lo, io.tw_hi, io.tw_mask, io.tw_sh,
+                                                         tg * (unsigned)(j + r * Ns)));
+            }
             C *dst = io.out + ((long)t * io.out_vs + (long)j * io.out_es);
             const long st = (long)Ns * io.out_es;
 #pragma unroll
-            for (int r = 0; r < R; r++) dst[r * st] = out_value(v[k][r], io.smask, io.has_scale, io.scale);
+            for (int r = 0; r < R; r++) dst[r * st] = out_value(v[k][r], io.smask_out, io.has_scale, io.scale);
         }
     }
 }
@@ -843,6 +878,18 @@ __global__ void __launch_bounds__(MAXT) k_smem(const __grid_constant__ SmemArgs<
         if (KIND == K_C2C && a.passes != 0 && cin.vec && cout.vec) {
             // c2c on interleaved views: first pass from the view, last pass to the view
             TileIO<T> io;
+            io.smask_in = a.conj_in ? 0x80000000u : 0u;
+            io.smask_out = a.conj_out ? 0x80000000u : 0u;
+            io.has_scale = a.has_scale != 0;
+            io.scale = a.has_scale ? a.scale : (T)1;
+            io.mnt = (nt == a.vpb) ? a.mvpb : magic_of((unsigned)nt);
+            io.tw_lo = a.tw_lo;
+            io.tw_hi = a.tw_hi;
+            io.tw_mask = a.tw_mask;
+            io.tw_sh = a.tw_sh;
+            const long by = blockIdx.y;
+            io.tw_t0 = (unsigned)(v0 * a.tw_ts + (a.y0 + by) * a.tw_ys);
+            io.tw_ts = a.tw_ts;
             if (a.tma) {
                 // column tile: TMA boxes of the vpb adjacent transforms land as n*vpb + t
                 __shared__ __align__(8) uint64_t tbar;
@@ -861,33 +908,27 @@ __global__ void __launch_bounds__(MAXT) k_smem(const __grid_constant__ SmemArgs<
                 }
                 io.in = nullptr;
                 io.in_es = io.in_vs = 0;
-                io.out = reinterpret_cast<C *>(cout.re) + (cout.off + v0 * cout.vs);
+                io.out = reinterpret_cast<C *>(cout.re) + (cout.off + v0 * cout.vs + by * a.bvs_out);
                 io.out_es = cout.es;
                 io.out_vs = cout.vs;
-                io.smask = a.inv ? 0x80000000u : 0u;
-                io.has_scale = a.has_scale != 0;
-                io.scale = a.has_scale ? a.scale : (T)1;
                 io.vf = true;
-                io.mnt = (nt == a.vpb) ? a.mvpb : magic_of((unsigned)nt);
+                io.vf_out = a.st_rows == 0;
                 // the conjugation of the inverse is folded into the first pass's
                 // input: flip the imaginary parts in place
-                if (a.inv)
+                if (a.conj_in)
                     for (int i = tid; i < a.tma_boxes * a.tma_rows * a.vpb; i += nthr) s[i].y = -s[i].y;
-                if (a.inv) __syncthreads();
+                if (a.conj_in) __syncthreads();
                 staged_tile<T, EMAX>(s, ld, nt, a.vpb, a.passes, a.twg, a.pc, io);
                 return;
             }
-            io.in = reinterpret_cast<const C *>(cin.re) + (cin.off + v0 * cin.vs);
-            io.out = reinterpret_cast<C *>(cout.re) + (cout.off + v0 * cout.vs);
+            io.in = reinterpret_cast<const C *>(cin.re) + (cin.off + v0 * cin.vs + by * a.bvs_in);
+            io.out = reinterpret_cast<C *>(cout.re) + (cout.off + v0 * cout.vs + by * a.bvs_out);
             io.in_es = cin.es;
             io.in_vs = cin.vs;
             io.out_es = cout.es;
             io.out_vs = cout.vs;
-            io.smask = a.inv ? 0x80000000u : 0u;
-            io.has_scale = a.has_scale != 0;
-            io.scale = a.has_scale ? a.scale : (T)1;
-            io.vf = a.vec_fast != 0;
-            io.mnt = (nt == a.vpb) ? a.mvpb : magic_of((unsigned)nt);
+            io.vf = a.vec_fast != 0 && a.ld_rows == 0;
+            io.vf_out = a.vec_fast != 0 && a.st_rows == 0;
             c2c_tile<T, EMAX>(s, ld, nt, a.passes, a.twg, a.pc, io);
             return;
         }
@@ -908,11 +949,12 @@ __global__ void __launch_bounds__(MAXT) k_smem(const __grid_constant__ SmemArgs<
             io.in_es = 1;
             io.in_vs = rin.vs / 2;
             io.out_es = io.out_vs = 0;
-            io.smask = 0u;
+            io.smask_in = io.smask_out = 0u;
             io.has_scale = false;
             io.scale = (T)1;
-            io.vf = false;
+            io.vf = io.vf_out = false;
             io.mnt = 0;
+            io.tw_lo = io.tw_hi = nullptr;
             tile_passes<T, EMAX, true, false>(s, ld, nt, a.passes, a.twg, a.pc, io);
         } else {
         if (KIND == K_C2C) {
@@ -961,11 +1003,13 @@ __global__ void __launch_bounds__(MAXT) k_smem(const __grid_constant__ SmemArgs<
             io.in_es = io.in_vs = 0;
             io.out_es = 1;
             io.out_vs = rout.vs / 2;
-            io.smask = 0x80000000u;
+            io.smask_in = 0u;
+            io.smask_out = 0x80000000u;
             io.has_scale = a.has_scale != 0;
             io.scale = a.has_scale ? a.scale : (T)1;
-            io.vf = false;
+            io.vf = io.vf_out = false;
             io.mnt = 0;
+            io.tw_lo = io.tw_hi = nullptr;
             tile_passes<T, EMAX, false, true>(s, ld, nt, a.passes, a.twg, a.pc, io);
             return;
         }

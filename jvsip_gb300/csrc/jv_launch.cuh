@@ -109,7 +109,9 @@ static bool tma_columns(SmemArgs<T> &a, const Job &j, long vpb, long ld) {
     // 4096 points 5-9 % faster with TMA boxes, 1000 points and shorter 10-30 %
     // slower than the first pass's own coalesced loads)
     const bool want = j.tma_columns == 1 || (j.tma_columns < 0 && j.N >= 1536);
-    if (!want || j.kind != K_C2C || !a.vec_fast || !a.cin.vec || !a.cout.vec || j.npass < 2) return false;
+    if (!want || j.kind != K_C2C || !a.vec_fast || a.ld_rows || !a.cin.vec || !a.cout.vec || j.npass < 2 ||
+        j.nbatch > 1)
+        return false;
     if (v.vs != 1 || v.es <= 0 || vpb % 2 != 0 || 2 * vpb > 256) return false;
     const T *base = (const T *)v.re + 2 * v.off;
     if (((uintptr_t)base % 16) || ((2 * v.es * (long)sizeof(T)) % 16)) return false;
@@ -219,9 +221,18 @@ static bool launch_smem_v(SmemArgs<T> &a, const Job &j, long vpb, long ld, cudaS
         set_error(E_UNSUPPORTED, "too many transforms for one launch");
         return false;
     }
-    k_smem<T, KIND, EMAX, MAXT><<<(unsigned)grid, (unsigned)nthr, smem, st>>>(a);
-    count_launch();
-    return cuda_ok(cudaGetLastError(), "k_smem launch");
+    // groups along y, at most 65535 per launch
+    for (long y0 = 0; y0 < j.nbatch; y0 += 65535) {
+        const long ny = std::min(65535L, j.nbatch - y0);
+        SmemArgs<T> b = a;
+        b.cin.off += y0 * a.bvs_in;
+        b.cout.off += y0 * a.bvs_out;
+        b.y0 = y0;
+        k_smem<T, KIND, EMAX, MAXT><<<dim3((unsigned)grid, (unsigned)ny), (unsigned)nthr, smem, st>>>(b);
+        count_launch();
+        if (!cuda_ok(cudaGetLastError(), "k_smem launch")) return false;
+    }
+    return true;
 }
 
 // The shared-memory kernel for transform kind KIND (one instantiation per
@@ -260,6 +271,24 @@ bool launch_smem_t(const Job &j, cudaStream_t st) {
     bool vf_in = labs_(vs_in) == 1 && labs_(es_in) != 1;
     bool vf_out = labs_(vs_out) == 1 && labs_(es_out) != 1;
     a.vec_fast = (vf_in || vf_out) ? 1 : 0;
+    // a row-contiguous side of a column-type tile keeps the element-fastest mapping
+    a.ld_rows = (a.vec_fast && !vf_in && labs_(es_in) == 1) ? 1 : 0;
+    a.st_rows = (a.vec_fast && !vf_out && labs_(es_out) == 1) ? 1 : 0;
+    a.conj_in = j.conj_in < 0 ? j.inv : j.conj_in;
+    a.conj_out = j.conj_out < 0 ? j.inv : j.conj_out;
+    a.bvs_in = j.bvs_in;
+    a.bvs_out = j.bvs_out;
+    a.tw_lo = (const C *)j.tw_lo;
+    a.tw_hi = (const C *)j.tw_hi;
+    a.tw_mask = j.tw_mask;
+    a.tw_sh = j.tw_sh;
+    a.tw_ts = j.tw_ts;
+    a.tw_ys = j.tw_ys;
+    if ((j.nbatch > 1 || j.tw_lo || a.conj_in != j.inv || a.conj_out != j.inv) &&
+        !(j.kind == K_C2C && a.cin.vec && a.cout.vec && j.npass > 0)) {
+        set_error(E_UNSUPPORTED, "long-transform step on a view the fused c2c tile does not take");
+        return false;
+    }
     {
         const RView &rv = (j.kind == K_R2C) ? j.rin : j.rout;
         a.real_pairs = (j.kind != K_C2C && !a.vec_fast && rv.rst == 1 && rv.es == 1 && rv.off % 2 == 0 &&
@@ -284,7 +313,7 @@ bool launch_smem_t(const Job &j, cudaStream_t st) {
         // with under four CTAs
         vpb = (sizeof(T) == 4) ? 16 : 8;
         const long minv = 32 / (long)sizeof(C);
-        while (vpb > minv && (j.nvec + vpb - 1) / vpb < 4L * d->sms) vpb /= 2;
+        while (vpb > minv && (j.nvec + vpb - 1) / vpb * j.nbatch < 4L * d->sms) vpb /= 2;
         if (ld % 2 == 0) ld += 1;
     } else {
         long target = (sizeof(T) == 4) ? 2048 : 1024;

@@ -319,12 +319,115 @@ static bool build_tables(Plan *p) {
     return true;
 }
 
+// ---------------------------------------------------------------- long transforms
+static void long_free(LongPlan *lp) {
+    if (!lp) return;
+    for (Plan *q : {lp->p1, lp->p2})
+        if (q) {
+            release_tables(q);
+            delete q;
+        }
+    dfree(lp->d_lo);
+    dfree(lp->d_hi);
+    dfree(lp->scratch);
+    delete lp;
+}
+
+// A c2c plan of n points for one step of a long transform (tables from the
+// shared cache); nullptr when n has no codelet schedule.
+template <typename T>
+static Plan *step_plan(long n, int prec) {
+    Plan *q = new (std::nothrow) Plan();
+    if (!q) return nullptr;
+    q->type = JV_CCFFTOP;
+    q->prec = prec;
+    q->M = 1;
+    q->N = q->MN = n;
+    q->mN = 1;
+    q->radix = pass_radices(n, &q->smooth, prec == P_F32 ? 1024 : 512);
+    if (!q->smooth || q->radix.empty() || !make_tables<T>(q)) {
+        if (q->smooth && !q->radix.empty()) {
+            dfree(q->d_tw);
+            dfree(q->d_thalf);
+            dfree(q->d_twp);
+            dfree(q->d_twg);
+            dfree(q->d_pc);
+        }
+        delete q;
+        return nullptr;
+    }
+    return q;
+}
+
+// The two-step decomposition N = N1 * N2 of a length longer than one CTA
+// takes: N1 <= N2 as close to sqrt(N) as the codelet schedules allow, both
+// within the shared-memory kernel.  Leaves p->lp null (the multi-pass global
+// path) when there is none.  Returns false only on allocation failure.
+template <typename T>
+static bool build_long(Plan *p) {
+    const long N = p->MN;
+    const long lim = smem_max_len(p->prec, K_C2C);
+    if (N <= lim || N >= (1L << 31)) return true;
+    const long maxt = p->prec == P_F32 ? 1024 : 512;
+    long best = 0;
+    for (long d = 2; d * d <= N; d++) {
+        if (N % d) continue;
+        const long e = N / d;
+        if (d > lim || e > lim) continue;
+        bool s1 = false, s2 = false;
+        pass_radices(d, &s1, maxt);
+        pass_radices(e, &s2, maxt);
+        if (s1 && s2) best = d;
+    }
+    if (!best) return true;
+    LongPlan *lp = new (std::nothrow) LongPlan();
+    if (!lp) return false;
+    lp->N1 = best;
+    lp->N2 = N / best;
+    lp->p1 = step_plan<T>(lp->N1, p->prec);
+    lp->p2 = step_plan<T>(lp->N2, p->prec);
+    if (!lp->p1 || !lp->p2) {
+        long_free(lp);
+        return !jvsip_gpu_last_error();
+    }
+    // W_N^m = lo[m mod L] * hi[m / L], L = 2^sh about sqrt(N)
+    unsigned bits = 0;
+    while ((1L << bits) < N) bits++;
+    lp->sh = (bits + 1) / 2;
+    const long L = 1L << lp->sh, H = (N + L - 1) / L;
+    lp->mask = (unsigned)(L - 1);
+    std::vector<T> lo(2 * L), hi(2 * H);
+    for (long r = 0; r < L; r++) {
+        double c, s;
+        unit_root(r % N, N, &c, &s);
+        lo[2 * r] = (T)c;
+        lo[2 * r + 1] = (T)s;
+    }
+    for (long q = 0; q < H; q++) {
+        double c, s;
+        unit_root((q * L) % N, N, &c, &s);
+        hi[2 * q] = (T)c;
+        hi[2 * q + 1] = (T)s;
+    }
+    lp->d_lo = dmalloc(lo.size() * sizeof(T));
+    lp->d_hi = dmalloc(hi.size() * sizeof(T));
+    if (!lp->d_lo || !lp->d_hi ||
+        !cuda_ok(cudaMemcpy(lp->d_lo, lo.data(), lo.size() * sizeof(T), cudaMemcpyHostToDevice), "twiddle upload") ||
+        !cuda_ok(cudaMemcpy(lp->d_hi, hi.data(), hi.size() * sizeof(T), cudaMemcpyHostToDevice), "twiddle upload")) {
+        long_free(lp);
+        return false;
+    }
+    p->lp = lp;
+    return true;
+}
+
 static void plan_free(Plan *p) {
     if (!p) return;
     Device *d = device();
     if (d) cudaStreamSynchronize(d->stream);
     for (CallGraph &g : p->graphs)
         if (g.exec) cudaGraphExecDestroy(g.exec);
+    long_free(p->lp);
     release_tables(p);
     delete p;
 }
@@ -403,6 +506,11 @@ static Plan *new_plan(int type, vsip_length M, vsip_length N, double scale, int 
         dfree(p->d_twp);
         dfree(p->d_twg);
         dfree(p->d_pc);
+        delete p;
+        return nullptr;
+    }
+    if (!build_long<T>(p)) {
+        release_tables(p);
         delete p;
         return nullptr;
     }

@@ -1,0 +1,157 @@
+"""Transforms longer than one CTA takes (N above the shared-memory kernel's
+limit, 2^a 3^b 5^c 7^d lengths) run as two steps of N = N1 * N2 points:
+single FFTs and fftm rows and columns, unit and non-unit strides, in place,
+inverse with a scale, single and double precision, against numpy's FP64 FFT
+at the acceptance tolerance (rel-L2 <= 1e-6 log2 N for _f, 1e-14 log2 N for
+_d); plans with ntimes == 0 capture the two steps as a CUDA graph and replay
+them with identical results."""
+import numpy as np
+import pytest
+
+import jvsip_gb300 as J
+
+pytestmark = pytest.mark.gpu
+
+
+def tol(N, dtype):
+    return (1e-6 if dtype == np.float32 else 1e-14) * np.log2(N)
+
+
+def interleave(z, dtype):
+    a = np.empty(2 * z.size, dtype)
+    a[0::2] = z.real.reshape(-1)
+    a[1::2] = z.imag.reshape(-1)
+    return a
+
+
+def cplx(a):
+    return a[0::2].astype(np.float64) + 1j * a[1::2].astype(np.float64)
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def rnd(n, seed):
+    g = np.random.default_rng(seed)
+    return g.standard_normal(n) + 1j * g.standard_normal(n)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f", "d"])
+@pytest.mark.parametrize("N", [16807 * 2, 32768, 40000, 65536, 3 ** 10, 2 ** 17, 5 ** 7, 7 ** 6, 1 << 20])
+def test_long_single_fft(N, dtype):
+    z = rnd(N, N)
+    x = interleave(z, dtype)
+    y = np.zeros_like(x)
+    bx, by = J.CBlock(x), J.CBlock(y)
+    bx.admit(True)
+    by.admit(False)
+    vx, vy = bx.vview(0, 1, N), by.vview(0, 1, N)
+    p = J.FFT(J.KIND_CCOP, N, 1.0, J.VSIP_FFT_FWD, dtype)
+    p.ccfftop(vx, vy)
+    by.sync()
+    assert rel(cplx(y), np.fft.fft(z)) <= tol(N, dtype)
+    q = J.FFT(J.KIND_CCIP, N, 1.0 / N, J.VSIP_FFT_INV, dtype)
+    q.ccfftip(vy)
+    by.release(True)
+    assert rel(cplx(y), z) <= 2 * tol(N, dtype)
+    for v in (vx, vy):
+        v.destroy()
+    bx.destroy()
+    by.destroy()
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f", "d"])
+@pytest.mark.parametrize("M,N", [(3, 65536), (8, 40000), (2, 1 << 18)])
+def test_long_fftm_rows_pitched(M, N, dtype):
+    """Rows with a pitch larger than the row, forward out of place and the
+    inverse with scale 1/N in place."""
+    pitch = N + 24
+    z = rnd(M * N, M + N).reshape(M, N)
+    buf = np.zeros((M, pitch), np.complex128)
+    buf[:, :N] = z
+    x = interleave(buf, dtype)
+    y = np.zeros_like(x)
+    bx, by = J.CBlock(x), J.CBlock(y)
+    bx.admit(True)
+    by.admit(True)
+    vx, vy = bx.view(0, pitch, M, 1, N), by.view(0, pitch, M, 1, N)
+    J.FFTM(J.KIND_CCOP, M, N, 1.0, J.VSIP_FFT_FWD, J.VSIP_ROW, dtype).ccfftmop(vx, vy)
+    by.sync()
+    Y = cplx(y).reshape(M, pitch)
+    assert rel(Y[:, :N], np.fft.fft(z, axis=1)) <= tol(N, dtype)
+    assert not Y[:, N:].any()
+    J.FFTM(J.KIND_CCIP, M, N, 1.0 / N, J.VSIP_FFT_INV, J.VSIP_ROW, dtype).ccfftmip(vy)
+    by.release(True)
+    assert rel(cplx(y).reshape(M, pitch)[:, :N], z) <= 2 * tol(N, dtype)
+    for v in (vx, vy):
+        v.destroy()
+    bx.destroy()
+    by.destroy()
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f", "d"])
+@pytest.mark.parametrize("N,M", [(65536, 16), (40000, 5), (32768, 64)])
+def test_long_fftm_columns(N, M, dtype):
+    """N-point transforms down the M columns of a row-major N x M matrix:
+    adjacent transforms are adjacent in memory."""
+    z = rnd(N * M, N * 7 + M).reshape(N, M)
+    x = interleave(z, dtype)
+    y = np.zeros_like(x)
+    bx, by = J.CBlock(x), J.CBlock(y)
+    bx.admit(True)
+    by.admit(False)
+    vx, vy = bx.view(0, M, N, 1, M), by.view(0, M, N, 1, M)
+    J.FFTM(J.KIND_CCOP, N, M, 1.0, J.VSIP_FFT_INV, J.VSIP_COL, dtype).ccfftmop(vx, vy)
+    by.sync()
+    assert rel(cplx(y).reshape(N, M), np.fft.ifft(z, axis=0) * N) <= tol(N, dtype)
+    for v in (vx, vy):
+        v.destroy()
+    bx.destroy()
+    by.destroy()
+
+
+@pytest.mark.parametrize("stride", [2, -3])
+def test_long_single_fft_strided(stride):
+    N = 65536
+    z = rnd(N, 11)
+    span = abs(stride) * (N - 1) + 1
+    off = 0 if stride > 0 else span - 1
+    buf = np.zeros(span + 4, np.complex128)
+    buf[off + stride * np.arange(N)] = z
+    x = interleave(buf, np.float32)
+    y = np.zeros(2 * N, np.float32)
+    bx, by = J.CBlock(x), J.CBlock(y)
+    vx, vy = bx.vview(off, stride, N), by.vview(0, 1, N)
+    J.FFT(J.KIND_CCOP, N, 0.5, J.VSIP_FFT_FWD).ccfftop(vx, vy)
+    assert rel(cplx(y), 0.5 * np.fft.fft(z)) <= tol(N, np.float32)
+    for v in (vx, vy):
+        v.destroy()
+    bx.destroy()
+    by.destroy()
+
+
+@pytest.mark.parametrize("N", [65536, 1 << 22])
+def test_long_plan_graph_replay(N):
+    z = rnd(N, 5)
+    x = interleave(z, np.float32)
+    y1, y2 = np.zeros_like(x), np.zeros_like(x)
+    bx, b1, b2 = J.CBlock(x), J.CBlock(y1), J.CBlock(y2)
+    for b in (bx, b1, b2):
+        b.admit(True)
+    many = J.FFT(J.KIND_CCOP, N, 1.0, J.VSIP_FFT_FWD, ntimes=0)
+    once = J.FFT(J.KIND_CCOP, N, 1.0, J.VSIP_FFT_FWD, ntimes=1)
+    vx, v1, v2 = bx.vview(0, 1, N), b1.vview(0, 1, N), b2.vview(0, 1, N)
+    for _ in range(4):
+        many.ccfftop(vx, v1)
+        once.ccfftop(vx, v2)
+    assert int(J.lib().jvsip_fftm_graphs(many.h)) == 1
+    assert int(J.lib().jvsip_fftm_graphs(once.h)) == 0
+    b1.sync()
+    b2.sync()
+    assert np.array_equal(y1, y2)
+    assert rel(cplx(y1), np.fft.fft(z)) <= tol(N, np.float32)
+    for v in (vx, v1, v2):
+        v.destroy()
+    for b in (bx, b1, b2):
+        b.destroy()

@@ -133,9 +133,9 @@ def test_many_times_plan_captures_graphs(N):
     ref = np.fft.fft(x[0::2].astype(np.float64) + 1j * x[1::2])
     got = y1[0::2] + 1j * y1[1::2].astype(np.float64)
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= 1e-6 * np.log2(N)
-    # calls of the shared-memory kernels are captured (from the second call
-    # on); the multi-pass path of long vectors allocates scratch and runs directly
-    assert graphs == (1 if N <= 16384 else 0)
+    # captured from the second call on (long vectors: the two steps, into the
+    # plan's scratch)
+    assert graphs == 1
     for w in (vx, v1, v2):
         w.destroy()
     for b in (bx, b1, b2):
