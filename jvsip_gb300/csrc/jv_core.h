@@ -146,6 +146,10 @@ struct LongPlan {
     size_t scratch_bytes = 0;
 };
 
+// Shortest length run as two steps when a plan has fewer transforms than half
+// the SMs (one CTA per transform would leave most of the GPU idle).
+constexpr long kLongFewMin = 8192;
+
 // Kernel entry points (defined in the kernel translation units).
 bool launch_smem_f32(const Job &j, cudaStream_t s);
 bool launch_smem_f64(const Job &j, cudaStream_t s);
@@ -157,6 +161,16 @@ bool launch_fast_f32(const Job &j, cudaStream_t s);   // specialised kernels; fa
 std::vector<int> fast_radices(long N);                // radix list of the specialised kernel for N
 bool launch_split_f32(const Job &j, cudaStream_t s);  // precision form; false when the call does not qualify
 int split_status_check(cudaStream_t s);               // device status of the precision form (0 = clean)
+// real long transforms: in-place Hermitian split of Z on an interleaved view,
+// C2R un-split into dense conjugated Y, and the final store of dense conjugated y
+bool launch_r2c_pairs_f32(void *z, long es, long vs, long N, long nvec, int has_scale, double scale,
+                          const void *thalf, cudaStream_t s);
+bool launch_r2c_pairs_f64(void *z, long es, long vs, long N, long nvec, int has_scale, double scale,
+                          const void *thalf, cudaStream_t s);
+bool launch_c2r_unsplit_f32(const Job &j, void *ydst, cudaStream_t s);
+bool launch_c2r_unsplit_f64(const Job &j, void *ydst, cudaStream_t s);
+bool launch_c2r_unpack_f32(const Job &j, const void *y, cudaStream_t s);
+bool launch_c2r_unpack_f64(const Job &j, const void *y, cudaStream_t s);
 int *kernel_status();                                 // device word a kernel sets when a bounded wait expired
 int kernel_status_check(cudaStream_t s);              // reads and clears it (0 = clean)
 

@@ -283,13 +283,118 @@ static bool step_job(Job &q, const Job &j, const Plan *sp) {
     return true;
 }
 
+// The two steps of one c2c transform family: N-point transforms of the view
+// `in` (nv of them) into the view `out`; conj_in / conj_out / scale as given.
+static bool two_steps(const Job &j, LongPlan *lp, const CView &in, const CView &out, long nv, int conj_in,
+                      int conj_out, int has_scale, double scale, char *sc, size_t esz, cudaStream_t st) {
+    const long N = j.N, N1 = lp->N1, N2 = lp->N2;
+    CView scv;
+    scv.re = sc;
+    scv.im = sc + esz;
+    scv.cst = 2;
+    scv.off = 0;
+    // transforms of a vector far apart in memory ("rows": |vs| != 1 or one
+    // vector): groups are the vectors, transforms inside a group are n1 (step
+    // A) / k2 (step B).  Adjacent vectors ("columns", |vs| == 1): groups are
+    // n1 / k2 and the transforms inside a group are the vectors, adjacent in
+    // memory; the scratch then holds [n1][k2][v].
+    const bool cols = nv > 1 && (in.vs == 1 || in.vs == -1);
+    Job a = j, b = j;
+    a.nvec = b.nvec = nv;
+    if (!step_job(a, j, lp->p2) || !step_job(b, j, lp->p1)) return false;
+    // step A: transform over n2 (N2 points, element n1 + N1*n2 of x)
+    a.cin = in;
+    a.cout = scv;
+    a.conj_in = conj_in;
+    a.conj_out = 0;
+    a.has_scale = 0;
+    a.scale = 1.0;
+    a.tw_lo = lp->d_lo;
+    a.tw_hi = lp->d_hi;
+    a.tw_mask = lp->mask;
+    a.tw_sh = lp->sh;
+    // step B: transform over n1 (N1 points) of the scratch, k1 to y[k2 + N2*k1]
+    b.cin = scv;
+    b.cout = out;
+    b.conj_in = 0;
+    b.conj_out = conj_out;
+    b.has_scale = has_scale;
+    b.scale = scale;
+    if (!cols) {
+        a.nvec = N1;
+        a.nbatch = nv;
+        a.cin.es = in.es * N1;
+        a.cin.vs = in.es;
+        a.bvs_in = in.vs;
+        a.cout.es = 1;
+        a.cout.vs = N2;
+        a.bvs_out = N;
+        a.tw_ts = 1;
+        a.tw_ys = 0;
+        b.nvec = N2;
+        b.nbatch = nv;
+        b.cin.es = N2;
+        b.cin.vs = 1;
+        b.bvs_in = N;
+        b.cout.es = out.es * N2;
+        b.cout.vs = out.es;
+        b.bvs_out = out.vs;
+    } else {
+        a.nvec = nv;
+        a.nbatch = N1;
+        a.cin.es = in.es * N1;
+        a.cin.vs = in.vs;
+        a.bvs_in = in.es;
+        a.cout.es = nv;
+        a.cout.vs = 1;
+        a.bvs_out = N2 * nv;
+        a.tw_ts = 0;
+        a.tw_ys = 1;
+        b.nvec = nv;
+        b.nbatch = N2;
+        b.cin.es = N2 * nv;
+        b.cin.vs = 1;
+        b.bvs_in = nv;
+        b.cout.es = out.es * N2;
+        b.cout.vs = out.vs;
+        b.bvs_out = out.es;
+    }
+    if (j.prec == P_F32) return launch_smem_f32(a, st) && launch_smem_f32(b, st);
+    return launch_smem_f64(a, st) && launch_smem_f64(b, st);
+}
+
+// A real view of unit stride, even offset and pitch, 2-element aligned, as
+// the interleaved complex view of its pairs (x_2n + i x_2n+1).
+static bool real_as_complex(const RView &r, long nvec, size_t esz, CView *c) {
+    if (r.rst != 1 || r.es != 1 || r.off % 2 != 0 || (nvec > 1 && r.vs % 2 != 0) ||
+        ((uintptr_t)r.a % (2 * esz)) != 0)
+        return false;
+    c->re = r.a;
+    c->im = (char *)r.a + esz;
+    c->cst = 2;
+    c->off = r.off / 2;
+    c->es = 1;
+    c->vs = r.vs / 2;
+    return true;
+}
+
+// The long-transform path (LongPlan): c2c on interleaved views; R2C from a
+// real view of unit stride into an interleaved spectrum (steps into the
+// output, then the in-place split); C2R from any spectrum view (un-split into
+// scratch, steps into the real output as complex pairs, or into scratch and
+// the final store).  Returns with *handled unset when the call does not
+// qualify (the multi-pass global path takes it).
 static bool run_long(Job &j, cudaStream_t st, bool *handled) {
     *handled = false;
     LongPlan *lp = j.lp;
     const size_t esz = j.prec == P_F32 ? sizeof(float) : sizeof(double);
-    if (!lp || j.kind != K_C2C || !interleaved(j.cin, esz) || !interleaved(j.cout, esz)) return false;
-    const long N = j.N, N1 = lp->N1, N2 = lp->N2, nv = j.nvec;
-    const size_t need = (size_t)nv * N * 2 * esz;
+    if (!lp) return false;
+    CView zin;
+    if (j.kind == K_C2C && !(interleaved(j.cin, esz) && interleaved(j.cout, esz))) return false;
+    if (j.kind == K_R2C && !(interleaved(j.cout, esz) && real_as_complex(j.rin, j.nvec, esz, &zin))) return false;
+    const long N = j.N, nv = j.nvec;
+    const size_t one = (size_t)nv * N * 2 * esz;
+    const size_t need = j.kind == K_C2R ? 2 * one : one;
     *handled = true;
     if (lp->scratch_bytes < need) {
         // held by the plan (a captured call replays into it)
@@ -302,76 +407,33 @@ static bool run_long(Job &j, cudaStream_t st, bool *handled) {
         }
     }
     char *sc = (char *)lp->scratch;
-    CView scv;
-    scv.re = sc;
-    scv.im = sc + esz;
-    scv.cst = 2;
-    scv.off = 0;
-    // transforms of a vector far apart in memory ("rows": |vs| != 1 or one
-    // vector): groups are the vectors, transforms inside a group are n1 (step
-    // A) / k2 (step B).  Adjacent vectors ("columns", |vs| == 1): groups are
-    // n1 / k2 and the transforms inside a group are the vectors, adjacent in
-    // memory; the scratch then holds [n1][k2][v].
-    const bool cols = nv > 1 && (j.cin.vs == 1 || j.cin.vs == -1);
-    Job a = j, b = j;
-    if (!step_job(a, j, lp->p2) || !step_job(b, j, lp->p1)) return false;
-    // step A: transform over n2 (N2 points, element n1 + N1*n2 of x)
-    a.cin = j.cin;
-    a.cout = scv;
-    a.conj_in = j.inv;
-    a.conj_out = 0;
-    a.has_scale = 0;
-    a.scale = 1.0;
-    a.tw_lo = lp->d_lo;
-    a.tw_hi = lp->d_hi;
-    a.tw_mask = lp->mask;
-    a.tw_sh = lp->sh;
-    // step B: transform over n1 (N1 points) of the scratch, k1 to y[k2 + N2*k1]
-    b.cin = scv;
-    b.cout = j.cout;
-    b.conj_in = 0;
-    b.conj_out = j.inv;
-    if (!cols) {
-        a.nvec = N1;
-        a.nbatch = nv;
-        a.cin.es = j.cin.es * N1;
-        a.cin.vs = j.cin.es;
-        a.bvs_in = j.cin.vs;
-        a.cout.es = 1;
-        a.cout.vs = N2;
-        a.bvs_out = N;
-        a.tw_ts = 1;
-        a.tw_ys = 0;
-        b.nvec = N2;
-        b.nbatch = nv;
-        b.cin.es = N2;
-        b.cin.vs = 1;
-        b.bvs_in = N;
-        b.cout.es = j.cout.es * N2;
-        b.cout.vs = j.cout.es;
-        b.bvs_out = j.cout.vs;
-    } else {
-        a.nvec = nv;
-        a.nbatch = N1;
-        a.cin.es = j.cin.es * N1;
-        a.cin.vs = j.cin.vs;
-        a.bvs_in = j.cin.es;
-        a.cout.es = nv;
-        a.cout.vs = 1;
-        a.bvs_out = N2 * nv;
-        a.tw_ts = 0;
-        a.tw_ys = 1;
-        b.nvec = nv;
-        b.nbatch = N2;
-        b.cin.es = N2 * nv;
-        b.cin.vs = 1;
-        b.bvs_in = nv;
-        b.cout.es = j.cout.es * N2;
-        b.cout.vs = j.cout.vs;
-        b.bvs_out = j.cout.es;
+    if (j.kind == K_C2C)
+        return two_steps(j, lp, j.cin, j.cout, nv, j.inv, j.inv, j.has_scale, j.scale, sc, esz, st);
+    if (j.kind == K_R2C) {
+        // Z = F(z) into the first N elements of each output vector, then the split
+        if (!two_steps(j, lp, zin, j.cout, nv, 0, 0, 0, 1.0, sc, esz, st)) return false;
+        void *z = (char *)j.cout.re + (size_t)j.cout.off * 2 * esz;
+        return j.prec == P_F32
+                   ? launch_r2c_pairs_f32(z, j.cout.es, j.cout.vs, N, nv, j.has_scale, j.scale, j.thalf, st)
+                   : launch_r2c_pairs_f64(z, j.cout.es, j.cout.vs, N, nv, j.has_scale, j.scale, j.thalf, st);
     }
-    if (j.prec == P_F32) return launch_smem_f32(a, st) && launch_smem_f32(b, st);
-    return launch_smem_f64(a, st) && launch_smem_f64(b, st);
+    // C2R: conj(Y) dense in the second half of the scratch, the steps, conj back
+    char *ys = sc + one;
+    CView yv;
+    yv.re = ys;
+    yv.im = ys + esz;
+    yv.cst = 2;
+    yv.off = 0;
+    yv.es = 1;
+    yv.vs = N;
+    bool ok = j.prec == P_F32 ? launch_c2r_unsplit_f32(j, ys, st) : launch_c2r_unsplit_f64(j, ys, st);
+    if (!ok) return false;
+    CView xo;
+    if (real_as_complex(j.rout, nv, esz, &xo))
+        return two_steps(j, lp, yv, xo, nv, 0, 1, j.has_scale, j.scale, sc, esz, st);
+    // other real views: the steps back into the second half, then the final store
+    if (!two_steps(j, lp, yv, yv, nv, 0, 0, 0, 1.0, sc, esz, st)) return false;
+    return j.prec == P_F32 ? launch_c2r_unpack_f32(j, ys, st) : launch_c2r_unpack_f64(j, ys, st);
 }
 
 static bool run_job(Job &j, cudaStream_t st) {
@@ -379,7 +441,10 @@ static bool run_job(Job &j, cudaStream_t st) {
     if (j.form == JVSIP_FORM_SPLIT_BF16 || j.form == JVSIP_FORM_SPLIT_FP16) {
         if (launch_split_f32(j, st)) return jvsip_gpu_last_error() == 0;
     }
-    if (job_in_smem(j)) {
+    // few transforms of a length with a decomposition: two steps over many
+    // CTAs instead of one CTA per transform
+    const bool few = j.lp && j.nvec * 2 < (long)device()->sms && j.N >= kLongFewMin;
+    if (job_in_smem(j) && !few) {
         if (j.prec == P_F32) {
             if (launch_fast_f32(j, st)) return true;
             return launch_smem_f32(j, st);
@@ -390,6 +455,13 @@ static bool run_job(Job &j, cudaStream_t st) {
         bool handled = false;
         const bool ok = run_long(j, st, &handled);
         if (handled) return ok;
+    }
+    if (job_in_smem(j)) {
+        if (j.prec == P_F32) {
+            if (launch_fast_f32(j, st)) return true;
+            return launch_smem_f32(j, st);
+        }
+        return launch_smem_f64(j, st);
     }
     return j.prec == P_F32 ? launch_global_f32(j, st) : launch_global_f64(j, st);
 }
@@ -419,9 +491,13 @@ static bool run_job_planned(Plan *p, Job &j, cudaStream_t st) {
     const bool split = (j.form == JVSIP_FORM_SPLIT_BF16 || j.form == JVSIP_FORM_SPLIT_FP16);
     // a long transform captures once its plan holds the scratch for this call
     const size_t esz = j.prec == P_F32 ? sizeof(float) : sizeof(double);
-    const bool long_ready = j.lp && j.kind == K_C2C && interleaved(j.cin, esz) && interleaved(j.cout, esz) &&
-                            j.lp->scratch_bytes >= (size_t)j.nvec * j.N * 2 * esz;
-    const bool long_job = j.lp && j.kind == K_C2C && interleaved(j.cin, esz) && interleaved(j.cout, esz);
+    CView tmpv;
+    const bool long_job = j.lp && ((j.kind == K_C2C && interleaved(j.cin, esz) && interleaved(j.cout, esz)) ||
+                                   (j.kind == K_R2C && interleaved(j.cout, esz) &&
+                                    real_as_complex(j.rin, j.nvec, esz, &tmpv)) ||
+                                   j.kind == K_C2R);
+    const bool long_ready =
+        long_job && j.lp->scratch_bytes >= (size_t)j.nvec * j.N * 2 * esz * (j.kind == K_C2R ? 2 : 1);
     if (!split && !job_in_smem(j) && !long_job) return run_job(j, st);
     CallGraph *e = nullptr;
     for (CallGraph &g : p->graphs)

@@ -1215,6 +1215,49 @@ __global__ void k_c2r_unsplit(const SplitArgs<T> a) {
     }
 }
 
+// R2C Hermitian split in place on an interleaved output view holding Z_k,
+// k < N (the two steps of a long transform wrote it there): the thread of pair
+// k (0 <= k <= N/2) reads Z_k and Z_{N-k} (Z_N = Z_0) and writes X_k and
+// X_{N-k} (X_N for k = 0), so no thread reads what another writes
+// (c_VSIP_src/VI_rcfftmop_f_def.h:79-118).
+template <typename T> struct PairSplitArgs {
+    typedef typename cplx_t<T>::t C;
+    C *z;           // element (v, k) at z[v*vs + k*es]
+    long es, vs;
+    int N;
+    long nvec;
+    int has_scale;
+    T scale;
+    const C *thalf;
+};
+
+template <typename T>
+__global__ void k_r2c_split_pairs(const PairSplitArgs<T> a) {
+    typedef typename cplx_t<T>::t C;
+    const int H = a.N / 2 + 1;
+    const long tot = a.nvec * H;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < tot; i += (long)gridDim.x * blockDim.x) {
+        const long v = i / H;
+        const int k = (int)(i - v * H);
+        C *row = a.z + v * a.vs;
+        const int nk = (k == 0) ? a.N : a.N - k;  // output index of the pair's second element
+        C zk = row[(long)k * a.es];
+        C zn = row[(long)(k == 0 ? 0 : a.N - k) * a.es];
+        if (a.has_scale) {
+            zk = cscale(zk, a.scale);
+            zn = cscale(zn, a.scale);
+        }
+        const C w = a.thalf[k], w2 = a.thalf[nk];
+        // X_k from f = Z_k, b = Z_{N-k}; X_{N-k} from f = Z_{N-k}, b = Z_k
+        const C xk = mk<C>((T)0.5 * (zn.x + zk.x + w.x * (zn.y + zk.y) + w.y * (zk.x - zn.x)),
+                           (T)0.5 * (zk.y - zn.y + w.x * (zn.x - zk.x) + w.y * (zn.y + zk.y)));
+        const C xn = mk<C>((T)0.5 * (zk.x + zn.x + w2.x * (zk.y + zn.y) + w2.y * (zn.x - zk.x)),
+                           (T)0.5 * (zn.y - zk.y + w2.x * (zk.x - zn.x) + w2.y * (zk.y + zn.y)));
+        row[(long)k * a.es] = xk;
+        if (nk != k) row[(long)nk * a.es] = xn;
+    }
+}
+
 // C2R final store from dense conjugated y: x_2n = Re, x_2n+1 = -Im (conj back), scaled.
 template <typename T> struct UnpackArgs {
     typedef typename cplx_t<T>::t C;

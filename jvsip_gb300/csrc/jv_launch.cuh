@@ -369,6 +369,56 @@ static unsigned grid_for(long total) {
     return (unsigned)g;
 }
 
+// Helper kernels of the real long transforms (two-step path).
+template <typename T>
+bool launch_r2c_pairs_t(void *z, long es, long vs, long N, long nvec, int has_scale, double scale,
+                        const void *thalf, cudaStream_t st) {
+    typedef typename cplx_t<T>::t C;
+    PairSplitArgs<T> a;
+    a.z = (C *)z;
+    a.es = es;
+    a.vs = vs;
+    a.N = (int)N;
+    a.nvec = nvec;
+    a.has_scale = has_scale;
+    a.scale = (T)scale;
+    a.thalf = (const C *)thalf;
+    k_r2c_split_pairs<T><<<grid_for<T>(nvec * (N / 2 + 1)), 256, 0, st>>>(a);
+    count_launch();
+    return cuda_ok(cudaGetLastError(), "k_r2c_split_pairs launch");
+}
+
+template <typename T>
+bool launch_c2r_unsplit_t(const Job &j, void *ydst, cudaStream_t st) {
+    typedef typename cplx_t<T>::t C;
+    SplitArgs<T> s;
+    memset(&s, 0, sizeof(s));
+    s.N = (int)j.N;
+    s.nvec = j.nvec;
+    s.zin = cacc<T>(j.cin);
+    s.ydst = (C *)ydst;
+    s.thalf = (const C *)j.thalf;
+    k_c2r_unsplit<T><<<grid_for<T>(j.nvec * j.N), 256, 0, st>>>(s);
+    count_launch();
+    return cuda_ok(cudaGetLastError(), "k_c2r_unsplit launch");
+}
+
+template <typename T>
+bool launch_c2r_unpack_t(const Job &j, const void *y, cudaStream_t st) {
+    typedef typename cplx_t<T>::t C;
+    UnpackArgs<T> u;
+    memset(&u, 0, sizeof(u));
+    u.N = (int)j.N;
+    u.nvec = j.nvec;
+    u.has_scale = j.has_scale;
+    u.scale = (T)j.scale;
+    u.y = (const C *)y;
+    u.xout = rsto<T>(j.rout);
+    k_c2r_unpack<T><<<grid_for<T>(j.nvec * j.N), 256, 0, st>>>(u);
+    count_launch();
+    return cuda_ok(cudaGetLastError(), "k_c2r_unpack launch");
+}
+
 // Global-memory path: one launch per radix pass, dense scratch between passes.
 template <typename T>
 bool launch_global_t(const Job &j, cudaStream_t st) {

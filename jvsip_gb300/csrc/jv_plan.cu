@@ -367,7 +367,10 @@ template <typename T>
 static bool build_long(Plan *p) {
     const long N = p->MN;
     const long lim = smem_max_len(p->prec, K_C2C);
-    if (N <= lim || N >= (1L << 31)) return true;
+    // lengths one CTA takes get the decomposition too when the plan has few
+    // transforms: one CTA per transform would leave most SMs idle
+    const bool few = p->mN * 2 < (long)device()->sms && N >= kLongFewMin;
+    if ((N <= lim && !few) || N >= (1L << 31)) return true;
     const long maxt = p->prec == P_F32 ? 1024 : 512;
     long best = 0;
     for (long d = 2; d * d <= N; d++) {

@@ -155,3 +155,62 @@ def test_long_plan_graph_replay(N):
         v.destroy()
     for b in (bx, b1, b2):
         b.destroy()
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f", "d"])
+@pytest.mark.parametrize("M,N,pitch", [(3, 1 << 17, 1 << 17), (2, 80000, 80010), (1, 1 << 20, 1 << 20)])
+def test_long_real_rows(M, N, pitch, dtype):
+    """R2C rows of N real points (half length N/2 beyond one CTA) into pitched
+    spectra, then C2R back with scale 1/N; the real rows have a pitch."""
+    H = N // 2 + 1
+    g = np.random.default_rng(N + M)
+    xr = g.standard_normal((M, N))
+    xb = np.zeros((M, pitch), dtype)
+    xb[:, :N] = xr
+    x = xb.reshape(-1).copy()
+    zp = H + 6
+    z = np.zeros(2 * M * zp, dtype)
+    back = np.zeros(M * pitch, dtype)
+    bx, bz, bb = J.RBlock(x), J.CBlock(z), J.RBlock(back)
+    for b in (bx, bz, bb):
+        b.admit(True)
+    vx, vz, vb = bx.view(0, pitch, M, 1, N), bz.view(0, zp, M, 1, H), bb.view(0, pitch, M, 1, N)
+    J.FFTM(J.KIND_RCOP, M, N, 1.0, J.VSIP_FFT_FWD, J.VSIP_ROW, dtype).rcfftmop(vx, vz)
+    J.FFTM(J.KIND_CROP, M, N, 1.0 / N, J.VSIP_FFT_INV, J.VSIP_ROW, dtype).crfftmop(vz, vb)
+    bz.sync()
+    bb.sync()
+    Z = cplx(z).reshape(M, zp)
+    assert rel(Z[:, :H], np.fft.rfft(xr, axis=1)) <= tol(N // 2, dtype)
+    assert not Z[:, H:].any()
+    B = back.reshape(M, pitch).astype(np.float64)
+    assert rel(B[:, :N], xr) <= 2 * tol(N // 2, dtype)
+    assert not B[:, N:].any()
+    for v in (vx, vz, vb):
+        v.destroy()
+    for b in (bx, bz, bb):
+        b.destroy()
+
+
+@pytest.mark.parametrize("stride", [2, -1])
+def test_long_real_vector_strided(stride):
+    """Real vectors of non-unit stride take the multi-pass path for R2C and
+    the two steps plus the final store for C2R."""
+    N = 1 << 16
+    g = np.random.default_rng(3 + stride)
+    xr = g.standard_normal(N)
+    span = abs(stride) * (N - 1) + 1
+    off = 0 if stride > 0 else span - 1
+    x = np.zeros(span, np.float32)
+    x[off + stride * np.arange(N)] = xr
+    z = np.zeros(2 * (N // 2 + 1), np.float32)
+    back = np.zeros(span, np.float32)
+    bx, bz, bb = J.RBlock(x), J.CBlock(z), J.RBlock(back)
+    vx, vz, vb = bx.vview(off, stride, N), bz.vview(0, 1, N // 2 + 1), bb.vview(off, stride, N)
+    J.FFT(J.KIND_RCOP, N, 1.0).rcfftop(vx, vz)
+    J.FFT(J.KIND_CROP, N, 1.0 / N).crfftop(vz, vb)
+    assert rel(cplx(z), np.fft.rfft(xr)) <= tol(N // 2, np.float32)
+    assert rel(back[off + stride * np.arange(N)].astype(np.float64), xr) <= 2 * tol(N // 2, np.float32)
+    for v in (vx, vz, vb):
+        v.destroy()
+    for b in (bx, bz, bb):
+        b.destroy()
