@@ -26,7 +26,8 @@ columns x 4096), cfg2rc / cfg2cr (4096 x 1536 real <-> 4096 x 769), cfg3d
 (16384 x 4096 c128), cfg4 (32768 x 1024, rows scaled by 10^U(-3,3)), cfg5
 (batching: uneven lengths and row counts in one launch vs a loop of per-plan
 calls), vec / vecd / vecrc (one single FFT of --points points: c64, c128,
-real f32 -> c64), measured the same way.
+real f32 -> c64), cols / rows (2^24 c64 points as --points-point transforms
+down the columns / along the rows of a matrix), measured the same way.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload NAME]
 
@@ -50,7 +51,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "batched FFT GB/s (% HBM peak): split-TC & batched vs plain FP32 at ≤1e-6 rel err"
 FALLBACK_HBM = 6800.0
-WORKLOADS = ["cfg3", "cfg1", "cfg2col", "cfg2rc", "cfg2cr", "cfg3d", "cfg4", "cfg5", "vec", "vecd", "vecrc"]
+WORKLOADS = ["cfg3", "cfg1", "cfg2col", "cfg2rc", "cfg2cr", "cfg3d", "cfg4", "cfg5", "vec", "vecd", "vecrc", "cols",
+             "rows"]
 
 
 def args():
@@ -69,7 +71,8 @@ def args():
     ap.add_argument("--no-autotune", action="store_true",
                     help="cfg5: use the cached or heuristic tiling (profiling runs: no tuner launches)")
     ap.add_argument("--batch-gb", type=float, default=2.0, help="cfg5: bytes per buffer of the instance sequence (0: the literal 20000 instances)")
-    ap.add_argument("--points", type=int, default=1 << 24, help="vec / vecd / vecrc: single-FFT length")
+    ap.add_argument("--points", type=int, default=1 << 24,
+                    help="vec / vecd / vecrc: single-FFT length; cols / rows: transform length (2^24 points in all)")
     return ap.parse_args()
 
 
@@ -336,6 +339,23 @@ def other_workload(a):
             call = lambda: L.vsip_crfftmop_f(plan.h, vx.h, vy.h)
             desc = "vsip_crfftmop_f 4096x769 c64 -> 4096x1536 f32 VSIP_ROW, scale 1/1536"
         nbytes, dt = M * (4 * N + 8 * H), "f32"
+    elif w in ("cols", "rows"):
+        # 2^24 points as n-point transforms down the columns / along the rows
+        n, tot = a.points, 1 << 24
+        other = tot // n
+        x = synth.fill(2 * tot, 9, 1)
+        y = np.zeros_like(x)
+        if w == "cols":
+            M, N = n, other
+            plan = J.FFTM(J.KIND_CCOP, M, N, 1.0, -1, J.VSIP_COL)
+        else:
+            M, N = other, n
+            plan = J.FFTM(J.KIND_CCOP, M, N, 1.0, -1, J.VSIP_ROW)
+        bx, by = J.CBlock(x), J.CBlock(y)
+        vx, vy = bx.view(0, N, M, 1, N), by.view(0, N, M, 1, N)
+        call = lambda: L.vsip_ccfftmop_f(plan.h, vx.h, vy.h)
+        nbytes, dt = 16 * tot, "f32"
+        desc = f"vsip_ccfftmop_f {M}x{N} c64 {'VSIP_COL' if w == 'cols' else 'VSIP_ROW'} ({n}-point transforms), N(0,1)"
     elif w in ("vec", "vecd", "vecrc"):
         # one single FFT of --points points (vsip_ccfftop / vsip_rcfftop)
         N = M = a.points
