@@ -27,7 +27,9 @@ columns x 4096), cfg2rc / cfg2cr (4096 x 1536 real <-> 4096 x 769), cfg3d
 (batching: uneven lengths and row counts in one launch vs a loop of per-plan
 calls), vec / vecd / vecrc (one single FFT of --points points: c64, c128,
 real f32 -> c64), cols / rows (2^24 c64 points as --points-point transforms
-down the columns / along the rows of a matrix), measured the same way.
+down the columns / along the rows of a matrix), komega (the k-omega power
+estimate of the reference's kw example on --kw-sensors x --kw-samples real
+data through jvsip_komega_f), measured the same way.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload NAME]
 
@@ -52,7 +54,7 @@ sys.path.insert(0, ROOT)
 METRIC = "batched FFT GB/s (% HBM peak): split-TC & batched vs plain FP32 at ≤1e-6 rel err"
 FALLBACK_HBM = 6800.0
 WORKLOADS = ["cfg3", "cfg1", "cfg2col", "cfg2rc", "cfg2cr", "cfg3d", "cfg4", "cfg5", "vec", "vecd", "vecrc", "cols",
-             "rows"]
+             "rows", "komega"]
 
 
 def args():
@@ -71,6 +73,8 @@ def args():
     ap.add_argument("--no-autotune", action="store_true",
                     help="cfg5: use the cached or heuristic tiling (profiling runs: no tuner launches)")
     ap.add_argument("--batch-gb", type=float, default=2.0, help="cfg5: bytes per buffer of the instance sequence (0: the literal 20000 instances)")
+    ap.add_argument("--kw-sensors", type=int, default=4096, help="komega: sensors (rows of the data)")
+    ap.add_argument("--kw-samples", type=int, default=4096, help="komega: samples per sensor (even)")
     ap.add_argument("--points", type=int, default=1 << 24,
                     help="vec / vecd / vecrc: single-FFT length; cols / rows: transform length (2^24 points in all)")
     return ap.parse_args()
@@ -305,6 +309,8 @@ def other_workload(a):
     w, f32 = a.workload, np.float32
     if w == "cfg5":
         return batching_workload(a, torch, J, L, ext)
+    if w == "komega":
+        return komega_workload(a, torch, J, L, ext)
     x = y = None
     if w in ("cfg1", "cfg2col", "cfg4"):
         M, N = (64, 1024) if w == "cfg1" else (1000, 4096) if w == "cfg2col" else (32768, 1024)
@@ -431,6 +437,83 @@ def other_workload(a):
         for name in extra.get("forms", {}):
             extra["forms"][name]["rel_l2_vs_fp64_oracle"] = extra["cpu_baseline"]["gpu_rel_l2_vs_fp64_oracle_" + name]
     print(json.dumps(line_for(a, nbytes / (ms / 1e3) / 1e9, ms, nbytes, dt, launches, extra)), flush=True)
+
+
+def komega_workload(a, torch, J, L, ext):
+    """The k-omega power estimate (kw.c komega(): tapers, R2C rows, c2c
+    columns, |.|^2, scale, accumulate) on Nsens x Nts real data through
+    jvsip_komega_f (two launches), blocks admitted.  Algorithmic bytes: the
+    data read and written back (8 B/sample), the spectrum written once and the
+    gram read and written (8 + 8 B/bin); the spectrum's round trip between the
+    two launches is not counted."""
+    import numpy as np
+    from jvsip_gb300 import synth
+    Ns, Nt = a.kw_sensors, a.kw_samples
+    Nf = Nt // 2 + 1
+    x = synth.fill(Ns * Nt, 11, 1)
+    x0 = x.copy()
+    f = np.zeros(2 * Ns * Nf, np.float32)
+    g = np.zeros(Ns * Nf, np.float32)
+    n = np.arange(1, Nt + 1, dtype=np.float64)
+    ts = (0.5 * (1 - np.cos(2 * np.pi * n / (Nt + 1)))).astype(np.float32)
+    m = np.arange(1, Ns + 1, dtype=np.float64)
+    arr = (0.5 * (1 - np.cos(2 * np.pi * m / (Ns + 1)))).astype(np.float32)
+    bx, bf, bg, bt, ba = J.RBlock(x), J.CBlock(f), J.RBlock(g), J.RBlock(ts), J.RBlock(arr)
+    for b in (bx, bf, bg, bt, ba):
+        b.admit(True)
+    vx, vf, vg = bx.view(0, Nt, Ns, 1, Nt), bf.view(0, 1, Ns, Ns, Nf), bg.view(0, 1, Ns, Ns, Nf)
+    vt, va = bt.vview(0, 1, Nt), ba.vview(0, 1, Ns)
+    rc = J.FFTM(J.KIND_RCOP, Ns, Nt, 1.0, J.VSIP_FFT_FWD, J.VSIP_ROW, ntimes=1)
+    cc = J.FFTM(J.KIND_CCIP, Ns, Nf, 1.0, J.VSIP_FFT_FWD, J.VSIP_COL, ntimes=1)
+    scale = 1.0 / 16
+
+    def call():
+        if L.jvsip_komega_f(rc.h, cc.h, vt.h, va.h, vx.h, vf.h, scale, vg.h):
+            raise RuntimeError("jvsip_komega_f: %s" % (J.last_error(),))
+
+    nbytes = 8 * Ns * Nt + 16 * Ns * Nf + 8 * Ns * Nf
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda") if nbytes < (512 << 20) else None
+    for _ in range(a.warmup):
+        call()
+    L.jvsip_gpu_synchronize()
+    n0 = L.jvsip_gpu_kernel_launches()
+    per = timed_calls(torch, ext, call, a.steps, flush)
+    launches = L.jvsip_gpu_kernel_launches() - n0
+    J.check("komega")
+    ms = statistics.mean(per)
+    extra = {"config": {"workload": f"jvsip_komega_f {Ns} sensors x {Nt} samples f32 (kw.c komega: tapers, "
+                                    f"rcfftmop ROW, ccfftmip COL, |.|^2, scale, accumulate), freq and gram "
+                                    f"column-major as kw.c creates them", "bytes_per_step": nbytes,
+                        "l2": "flushed between calls" if flush is not None else "inputs larger than L2"}}
+    # one call from the original data, checked against the oracle on the host
+    bx.release(False)
+    bg.release(False)
+    x[:] = x0
+    g[:] = 0
+    bx.admit(True)
+    bg.admit(True)
+    call()
+    for b in (bx, bf, bg):
+        b.release(True)
+    if not a.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle as O
+        d = O.RView(x0.copy(), 0, Nt, Ns, 1, Nt)
+        fo = O.CView(np.zeros_like(f), 0, 1, Ns, Ns, Nf)
+        go = O.RView(np.zeros_like(g), 0, 1, Ns, Ns, Nf)
+        t0 = time.perf_counter()
+        O.komega_f(ts, arr, d, fo, go, np.float32(scale))
+        cpu_s = time.perf_counter() - t0
+        extra["cpu_baseline"] = {"value": round(nbytes / cpu_s / 1e9, 3), "unit": "GB/s", "cores": 1,
+                                 "kind": "port", "sample": "the whole call once (the oracle's kw.c sequence)"}
+        extra["data_bit_exact_vs_oracle"] = bool(np.array_equal(x, d.buf))
+        ref = go.buf.astype(np.float64)
+        extra["gram_rel_l2_vs_oracle"] = float(np.linalg.norm(g - ref) / np.linalg.norm(ref))
+    for v in (vx, vf, vg, vt, va):
+        v.destroy()
+    for b in (bx, bf, bg, bt, ba):
+        b.destroy()
+    print(json.dumps(line_for(a, nbytes / (ms / 1e3) / 1e9, ms, nbytes, "f32", launches, extra)), flush=True)
 
 
 def batching_workload(a, torch, J, L, ext):

@@ -394,6 +394,28 @@ long jvsip_fftm_jofk(const void *plan, unsigned long *out, long cap);
  * invalid plan. */
 int  jvsip_fftm_graphs(const void *plan);
 
+/* The k-omega power estimate of the reference's kw example
+ * (examples/komegaExamples/kw_c/kw.c:8-26, komega()) in two launches instead
+ * of seven library passes.  With Nsens x Nts real data, rcfftm a VSIP_ROW
+ * rcfftmop _f plan (Nsens, Nts) and ccfftm a VSIP_COL ccfftm(ip|op) _f plan
+ * (Nsens, Nts/2+1), it leaves exactly what kw.c's sequence
+ *   vsip_vmmul_f(ts_taper, data, VSIP_ROW, data);
+ *   vsip_vmmul_f(array_taper, data, VSIP_COL, data);
+ *   vsip_rcfftmop_f(rcfftm, data, freq);  vsip_ccfftmip_f(ccfftm, freq);
+ *   vsip_mcmagsq_f(freq, real(freq));     vsip_smmul_f(scale, real(freq), real(freq));
+ *   vsip_madd_f(real(freq), gram, gram);
+ * leaves: data tapered in place, freq = (scale*|X|^2, Im X), gram += scale*|X|^2
+ * (tapers and power rounded in the reference's order; the transforms within
+ * the fftm tolerance).  The R2C's first pass tapers the rows as it loads them
+ * and the column transform's last pass stores the power and accumulates the
+ * gram.  All blocks must be admitted; data rows of unit stride with an even
+ * offset and pitch; freq interleaved.  Returns 0, or the error code also
+ * recorded for jvsip_gpu_last_error(). */
+int jvsip_komega_f(const vsip_fftm_f *rcfftm, const vsip_fftm_f *ccfftm,
+                   const vsip_vview_f *ts_taper, const vsip_vview_f *array_taper,
+                   const vsip_mview_f *data, const vsip_cmview_f *freq,
+                   vsip_scalar_f scale, const vsip_mview_f *gram);
+
 /* Complex-to-complex multiple FFT that allocates nothing (no counterpart in
  * the reference).  For callers that cannot allocate device memory when they
  * transform: code running during CUDA stream capture, real-time threads that

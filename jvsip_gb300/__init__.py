@@ -61,6 +61,7 @@ EXPORTS = [
     "vsip_cvcreate_f", "vsip_cvcreate_d", "vsip_vcreate_f", "vsip_vcreate_d",
     "vsip_cvdestroy_f", "vsip_cvdestroy_d", "vsip_vdestroy_f", "vsip_vdestroy_d",
     "vsip_cvalldestroy_f", "vsip_cvalldestroy_d", "vsip_valldestroy_f", "vsip_valldestroy_d",
+    "jvsip_komega_f",
 ]
 
 
@@ -200,6 +201,7 @@ def lib(load_only: bool = False):
     L.jvsip_fftm_passes.argtypes = [vp, C.POINTER(C.c_int), C.c_int]
     L.jvsip_fftm_graphs.argtypes = [vp]
     L.jvsip_fftm_graphs.restype = C.c_int
+    L.jvsip_komega_f.argtypes = [vp, vp, vp, vp, vp, vp, C.c_float, vp]
     L.jvsip_fftm_jofk.restype = C.c_long
     L.jvsip_fftm_jofk.argtypes = [vp, C.POINTER(C.c_ulong), C.c_long]
     _lib = L

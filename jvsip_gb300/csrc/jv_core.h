@@ -118,6 +118,17 @@ struct Job {
     const void *tw_hi = nullptr;       //   group*tw_ys: tw_lo[m & tw_mask] * tw_hi[m >> tw_sh]
     unsigned tw_mask = 0, tw_sh = 0, tw_ts = 0, tw_ys = 0;
     struct LongPlan *lp = nullptr;     // the plan's long-transform decomposition (or null)
+    // the k-omega pipeline (its own kernel instances): R2C rows tapered as they
+    // are loaded -- real element n of transform t times taper_n[n*taper_n_st],
+    // then times taper_t[t*taper_t_st], written back when taper_back -- and c2c
+    // columns storing (gram_scale*|X|^2, Im X) with gram[t*gram_vs + k*gram_es]
+    // += gram_scale*|X|^2
+    const void *taper_n = nullptr, *taper_t = nullptr;
+    long taper_n_st = 1, taper_t_st = 1;
+    int taper_back = 0;
+    void *gram = nullptr;
+    long gram_es = 0, gram_vs = 0;
+    double gram_scale = 1.0;
 };
 
 // A device-resident call of a plan captured into a CUDA graph: plans created
@@ -154,6 +165,8 @@ constexpr long kLongFewMin = 8192;
 bool launch_smem_f32(const Job &j, cudaStream_t s);
 bool launch_smem_f64(const Job &j, cudaStream_t s);
 bool launch_smem_real_f32(const Job &j, cudaStream_t s);  // R2C / C2R instances
+bool launch_komega_r2c_f32(const Job &j, cudaStream_t s); // tapered R2C rows (taper_* set)
+bool launch_komega_power_f32(const Job &j, cudaStream_t s); // c2c columns accumulating power (gram set)
 bool launch_smem_real_f64(const Job &j, cudaStream_t s);
 bool launch_global_f32(const Job &j, cudaStream_t s);
 bool launch_global_f64(const Job &j, cudaStream_t s);

@@ -434,6 +434,17 @@ template <typename T> struct SmemArgs {
     const typename cplx_t<T>::t *tw_lo, *tw_hi;
     unsigned tw_mask, tw_sh, tw_ts, tw_ys;
     long y0;          // group index of this launch's first group
+    // the k-omega pipeline's fused prologue / epilogue (instances KX_R2C_TAPER,
+    // KX_C2C_POWER only): real element n of transform t is multiplied by
+    // tp_n[n*tp_n_st] and then by tp_t[t*tp_t_st] as it is loaded (and written
+    // back when tp_back); output element k of transform t stores
+    // (g_scale*|X|^2, Im X) and adds g_scale*|X|^2 to gram[t*g_vs + k*g_es]
+    const T *tp_n, *tp_t;
+    long tp_n_st, tp_t_st;
+    int tp_back;
+    T *gram;
+    long g_es, g_vs;
+    T g_scale;
     CUtensorMap tmap;
     WalkConst win, wout;  // load / store walker constants for full tiles of vpb transforms
     CAcc<T> cin;
@@ -550,6 +561,12 @@ __device__ __forceinline__ C out_value(C v, unsigned smask, bool has_scale, T sc
     return v;
 }
 
+// single roundings without contraction into fused multiply-adds
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+
 template <typename T> struct TileIO {
     typedef typename cplx_t<T>::t C;
     const C *in;     // interleaved input; element (t, n) at in[t*in_vs + n*in_es]
@@ -564,7 +581,43 @@ template <typename T> struct TileIO {
     // output twiddle W^(g*k), g = tw_t0 + t*tw_ts (none when tw_lo is null)
     const C *tw_lo, *tw_hi;
     unsigned tw_mask, tw_sh, tw_t0, tw_ts;
+    // fused prologue / epilogue of the k-omega pipeline (FX template flag of
+    // the passes): tapers of the loaded real pairs (element and transform),
+    // the write-back target of the tapered input, and the power accumulator
+    const T *tp_n, *tp_t;
+    long tp_n_st, tp_t_st;
+    C *wb;
+    T *gram;
+    long g_es, g_vs;
+    T g_scale;
 };
+
+// FX flags of the fused passes
+constexpr int FX_TAPER = 1;  // first pass: taper the loaded real pairs, optionally write them back
+constexpr int FX_POWER = 2;  // last pass: store (s|X|^2, Im X), gram += s|X|^2
+
+// the tapered pair at complex index n of transform t: x_2n*tp_n[2n] then
+// *tp_t[t] (c_VSIP_src/vsip_vmmul_f.c: rows by the time taper, then columns by
+// the array taper; products rounded in that order)
+template <typename C, typename T>
+__device__ __forceinline__ C taper_pair(C c, const TileIO<T> &io, long n, int t) {
+    const T wt = io.tp_t[(long)t * io.tp_t_st];
+    const T w0 = io.tp_n[2 * n * io.tp_n_st], w1 = io.tp_n[(2 * n + 1) * io.tp_n_st];
+    c.x = mul_rn(mul_rn(w0, c.x), wt);
+    c.y = mul_rn(mul_rn(w1, c.y), wt);
+    return c;
+}
+
+// p = |v|^2 (c_VSIP_src/vsip_mcmagsq_f.c), p *= s (vsip_smmul_f.c),
+// gram = p + gram (vsip_madd_f.c), each rounded in that order; stores (p, Im v)
+template <typename C, typename T>
+__device__ __forceinline__ C power_out(C v, const TileIO<T> &io, long t, long k) {
+    T p = add_rn(mul_rn(v.x, v.x), mul_rn(v.y, v.y));
+    p = mul_rn(io.g_scale, p);
+    T *g = io.gram + t * io.g_vs + k * io.g_es;
+    *g = add_rn(p, *g);
+    return mk<C>(p, v.y);
+}
 
 // W^m from the two-level table of a long transform's output twiddles
 template <typename C>
@@ -585,7 +638,7 @@ __device__ __forceinline__ void tile_tj(int b, bool vf, int nt, unsigned mnt, in
 
 // First pass (Ns = 1, no twiddle) from global memory; to shared memory, or,
 // for a one-pass schedule (LAST), straight back to global memory.
-template <typename T, int R, int EMAX, bool LAST>
+template <typename T, int R, int EMAX, bool LAST, int FX = 0>
 __device__ __forceinline__ void pass_first(typename cplx_t<T>::t *s, int ld, int nt, const uint4 pc,
                                            const TileIO<T> &io) {
     typedef typename cplx_t<T>::t C;
@@ -604,6 +657,10 @@ __device__ __forceinline__ void pass_first(typename cplx_t<T>::t *s, int ld, int
 #pragma unroll
             for (int r = 0; r < R; r++) {
                 C c = src[r * st];
+                if constexpr ((FX & FX_TAPER) != 0) {
+                    c = taper_pair(c, io, (long)(j + r * NR), t);
+                    if (io.wb) io.wb[(long)t * io.in_vs + (long)(j + r * NR) * io.in_es] = c;
+                }
                 c.y = flip_sign(c.y, io.smask_in);
                 v[k][r] = c;
             }
@@ -620,8 +677,11 @@ __device__ __forceinline__ void pass_first(typename cplx_t<T>::t *s, int ld, int
                 // one pass: N = R, j = 0, output element r
                 C *dst = io.out + (long)t * io.out_vs;
 #pragma unroll
-                for (int r = 0; r < R; r++)
-                    dst[r * io.out_es] = out_value(v[k][r], io.smask_out, io.has_scale, io.scale);
+                for (int r = 0; r < R; r++) {
+                    C o = out_value(v[k][r], io.smask_out, io.has_scale, io.scale);
+                    if constexpr ((FX & FX_POWER) != 0) o = power_out(o, io, (long)t, (long)r);
+                    dst[r * io.out_es] = o;
+                }
             } else {
                 C *dst = s + t * ld;
 #pragma unroll
@@ -633,7 +693,7 @@ __device__ __forceinline__ void pass_first(typename cplx_t<T>::t *s, int ld, int
 }
 
 // Last pass (Ns = N/R, so m = j) from shared memory to global memory.
-template <typename T, int R, int EMAX>
+template <typename T, int R, int EMAX, int FX = 0>
 __device__ __forceinline__ void pass_last(const typename cplx_t<T>::t *s, int ld, int nt, int Ns,
                                           const typename cplx_t<T>::t *__restrict__ tp, const uint4 pc,
                                           const TileIO<T> &io) {
@@ -675,7 +735,11 @@ __device__ __forceinline__ void pass_last(const typename cplx_t<T>::t *s, int ld
             C *dst = io.out + ((long)t * io.out_vs + (long)j * io.out_es);
             const long st = (long)Ns * io.out_es;
 #pragma unroll
-            for (int r = 0; r < R; r++) dst[r * st] = out_value(v[k][r], io.smask_out, io.has_scale, io.scale);
+            for (int r = 0; r < R; r++) {
+                C o = out_value(v[k][r], io.smask_out, io.has_scale, io.scale);
+                if constexpr ((FX & FX_POWER) != 0) o = power_out(o, io, (long)t, (long)(j + r * Ns));
+                dst[r * st] = o;
+            }
         }
     }
 }
@@ -700,7 +764,7 @@ __device__ __forceinline__ void pass_last(const typename cplx_t<T>::t *s, int ld
 // The passes of a tile with the first pass reading the view (FROMG) and/or the
 // last pass writing the view (TOG) through io; otherwise those passes run in
 // shared memory like the middle ones.  The schedule must have at least one pass.
-template <typename T, int EMAX, bool FROMG, bool TOG>
+template <typename T, int EMAX, bool FROMG, bool TOG, int FX = 0>
 __device__ __forceinline__ void tile_passes(typename cplx_t<T>::t *s, int ld, int nt, unsigned long long packed,
                                             const typename cplx_t<T>::t *__restrict__ twg,
                                             const uint4 *__restrict__ pc, const TileIO<T> &io) {
@@ -720,13 +784,13 @@ __device__ __forceinline__ void tile_passes(typename cplx_t<T>::t *s, int ld, in
     if (FROMG) {
         const uint4 pc0 = __ldg(&pc[0]);
         if (TOG && np == 1) {
-#define JV_ONE(R) pass_first<T, R, EMAX, true>(s, ld, nt, pc0, io)
+#define JV_ONE(R) pass_first<T, R, EMAX, true, FX>(s, ld, nt, pc0, io)
             JV_RADIX_SWITCH(fi, JV_ONE)
 #undef JV_ONE
             return;
         }
         int Rf = 2;
-#define JV_FIRST(R) (pass_first<T, R, EMAX, false>(s, ld, nt, pc0, io), Rf = R)
+#define JV_FIRST(R) (pass_first<T, R, EMAX, false, FX>(s, ld, nt, pc0, io), Rf = R)
         JV_RADIX_SWITCH(fi, JV_FIRST)
 #undef JV_FIRST
         Ns = Rf;
@@ -739,23 +803,23 @@ __device__ __forceinline__ void tile_passes(typename cplx_t<T>::t *s, int ld, in
     smem_passes_from<T, EMAX>(s, ld, nt, mid, tp, pc, Ns, p);
     if (TOG && np > 0) {
         const uint4 pcl = __ldg(&pc[p]);
-#define JV_LAST(R) pass_last<T, R, EMAX>(s, ld, nt, Ns, tp, pcl, io)
+#define JV_LAST(R) pass_last<T, R, EMAX, FX>(s, ld, nt, Ns, tp, pcl, io)
         JV_RADIX_SWITCH(li, JV_LAST)
 #undef JV_LAST
     }
 }
 
-template <typename T, int EMAX>
+template <typename T, int EMAX, int FX = 0>
 __device__ __forceinline__ void c2c_tile(typename cplx_t<T>::t *s, int ld, int nt, unsigned long long packed,
                                          const typename cplx_t<T>::t *__restrict__ twg,
                                          const uint4 *__restrict__ pc, const TileIO<T> &io) {
-    tile_passes<T, EMAX, true, true>(s, ld, nt, packed, twg, pc, io);
+    tile_passes<T, EMAX, true, true, FX>(s, ld, nt, packed, twg, pc, io);
 }
 
 // A c2c tile whose input arrived in shared memory as n*dp + t (TMA boxes of
 // adjacent transforms): the first pass reads that order, the last pass
 // writes the view.  The schedule must have at least two passes.
-template <typename T, int EMAX>
+template <typename T, int EMAX, int FX = 0>
 __device__ __forceinline__ void staged_tile(typename cplx_t<T>::t *s, int ld, int nt, int dp, unsigned long long packed,
                                             const typename cplx_t<T>::t *__restrict__ twg,
                                             const uint4 *__restrict__ pc, const TileIO<T> &io) {
@@ -776,7 +840,7 @@ __device__ __forceinline__ void staged_tile(typename cplx_t<T>::t *s, int ld, in
     const unsigned long long mid = packed - (1ull << (4 * fi)) - (1ull << (4 * li));
     smem_passes_from<T, EMAX>(s, ld, nt, mid, tp, pc, Ns, p);
     const uint4 pcl = __ldg(&pc[p]);
-#define JV_LAST(R) pass_last<T, R, EMAX>(s, ld, nt, Ns, tp, pcl, io)
+#define JV_LAST(R) pass_last<T, R, EMAX, FX>(s, ld, nt, Ns, tp, pcl, io)
     JV_RADIX_SWITCH(li, JV_LAST)
 #undef JV_LAST
 }
@@ -854,9 +918,15 @@ __device__ __forceinline__ void tile_load(Walk &w, bool vf, int tot, C *s, int l
     }
 }
 
-template <typename T, int KIND, int EMAX, int MAXT>
+// Instances of the shared-memory kernel beyond the three transform kinds:
+// the k-omega pipeline's tapered R2C rows and power-accumulating c2c columns.
+constexpr int KX_R2C_TAPER = 3, KX_C2C_POWER = 4;
+
+template <typename T, int KIND0, int EMAX, int MAXT>
 __global__ void __launch_bounds__(MAXT) k_smem(const __grid_constant__ SmemArgs<T> a) {
     typedef typename cplx_t<T>::t C;
+    constexpr int KIND = KIND0 == KX_R2C_TAPER ? K_R2C : KIND0 == KX_C2C_POWER ? K_C2C : KIND0;
+    constexpr int FX = KIND0 == KX_R2C_TAPER ? FX_TAPER : KIND0 == KX_C2C_POWER ? FX_POWER : 0;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     C *s = reinterpret_cast<C *>(smem_raw);
     const int N = a.N, ld = a.ld;
@@ -890,6 +960,12 @@ __global__ void __launch_bounds__(MAXT) k_smem(const __grid_constant__ SmemArgs<
             const long by = blockIdx.y;
             io.tw_t0 = (unsigned)(v0 * a.tw_ts + (a.y0 + by) * a.tw_ys);
             io.tw_ts = a.tw_ts;
+            if constexpr ((FX & FX_POWER) != 0) {
+                io.gram = a.gram + v0 * a.g_vs;
+                io.g_es = a.g_es;
+                io.g_vs = a.g_vs;
+                io.g_scale = a.g_scale;
+            }
             if (a.tma) {
                 // column tile: TMA boxes of the vpb adjacent transforms land as n*vpb + t
                 __shared__ __align__(8) uint64_t tbar;
@@ -918,7 +994,7 @@ __global__ void __launch_bounds__(MAXT) k_smem(const __grid_constant__ SmemArgs<
                 if (a.conj_in)
                     for (int i = tid; i < a.tma_boxes * a.tma_rows * a.vpb; i += nthr) s[i].y = -s[i].y;
                 if (a.conj_in) __syncthreads();
-                staged_tile<T, EMAX>(s, ld, nt, a.vpb, a.passes, a.twg, a.pc, io);
+                staged_tile<T, EMAX, FX>(s, ld, nt, a.vpb, a.passes, a.twg, a.pc, io);
                 return;
             }
             io.in = reinterpret_cast<const C *>(cin.re) + (cin.off + v0 * cin.vs + by * a.bvs_in);
@@ -929,7 +1005,7 @@ __global__ void __launch_bounds__(MAXT) k_smem(const __grid_constant__ SmemArgs<
             io.out_vs = cout.vs;
             io.vf = a.vec_fast != 0 && a.ld_rows == 0;
             io.vf_out = a.vec_fast != 0 && a.st_rows == 0;
-            c2c_tile<T, EMAX>(s, ld, nt, a.passes, a.twg, a.pc, io);
+            c2c_tile<T, EMAX, FX>(s, ld, nt, a.passes, a.twg, a.pc, io);
             return;
         }
         // ---------------- load phase
@@ -955,7 +1031,14 @@ __global__ void __launch_bounds__(MAXT) k_smem(const __grid_constant__ SmemArgs<
             io.vf = io.vf_out = false;
             io.mnt = 0;
             io.tw_lo = io.tw_hi = nullptr;
-            tile_passes<T, EMAX, true, false>(s, ld, nt, a.passes, a.twg, a.pc, io);
+            if constexpr ((FX & FX_TAPER) != 0) {
+                io.tp_n = a.tp_n;
+                io.tp_n_st = a.tp_n_st;
+                io.tp_t = a.tp_t + v0 * a.tp_t_st;
+                io.tp_t_st = a.tp_t_st;
+                io.wb = a.tp_back ? const_cast<C *>(io.in) : nullptr;
+            }
+            tile_passes<T, EMAX, true, false, FX>(s, ld, nt, a.passes, a.twg, a.pc, io);
         } else {
         if (KIND == K_C2C) {
             walk_tile(w, vf, nt, N, cin.vs, cin.es, cin.off + v0 * cin.vs, win, exact);

@@ -290,11 +290,35 @@ bool launch_smem_t(const Job &j, cudaStream_t st) {
         return false;
     }
     {
+        // the real side of R2C (input) / C2R (output) read or written as complex
+        // pairs by the first / last pass with consecutive threads on consecutive
+        // elements: the real rows must not be the column-type side of the tile
         const RView &rv = (j.kind == K_R2C) ? j.rin : j.rout;
-        a.real_pairs = (j.kind != K_C2C && !a.vec_fast && rv.rst == 1 && rv.es == 1 && rv.off % 2 == 0 &&
+        const bool real_rows = (j.kind == K_R2C) ? !vf_in : !vf_out;
+        a.real_pairs = (j.kind != K_C2C && real_rows && rv.rst == 1 && rv.es == 1 && rv.off % 2 == 0 &&
                         rv.vs % 2 == 0 && rv.vs > 0 && ((uintptr_t)rv.a % (2 * sizeof(T))) == 0)
                            ? 1
                            : 0;
+    }
+    // the k-omega pipeline's tapers and power accumulator (their instances only)
+    a.tp_n = (const T *)j.taper_n;
+    a.tp_n_st = j.taper_n_st;
+    a.tp_t = (const T *)j.taper_t;
+    a.tp_t_st = j.taper_t_st;
+    a.tp_back = j.taper_back;
+    a.gram = (T *)j.gram;
+    a.g_es = j.gram_es;
+    a.g_vs = j.gram_vs;
+    a.g_scale = (T)j.gram_scale;
+    // the pipeline instances run only on their fused paths (the view walkers
+    // know neither tapers nor the power store)
+    if (KIND == KX_R2C_TAPER && !a.real_pairs) {
+        set_error(E_UNSUPPORTED, "tapered R2C needs real rows of unit stride, even offset and pitch");
+        return false;
+    }
+    if (KIND == KX_C2C_POWER && !(a.cin.vec && a.cout.vec)) {
+        set_error(E_UNSUPPORTED, "power columns need an interleaved spectrum");
+        return false;
     }
     const long N = j.N;
     // shared-memory rows are indexed i + i/16 (conflict-free Stockham passes)

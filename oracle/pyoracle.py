@@ -240,3 +240,26 @@ def ccfftm_rows_mt(x: np.ndarray, dir: int, scale: float, threads: int) -> np.nd
     if rc:
         raise RuntimeError("oracle multi-threaded run failed")
     return y
+
+
+def komega_f(ts, arr, data: RView, freq: CView, gram: RView, scale) -> None:
+    """The k-omega step of the reference's kw example (kw.c:8-26) restated:
+    the tapers (c_VSIP_src/vsip_vmmul_f.c, ROW then COL: ts[j]*d, then
+    arr[i]*(.)), the fftm oracle's rcfftmop (ROW) and ccfftmip (COL, forward,
+    scale 1), then |X|^2 as re*re + im*im (vsip_mcmagsq_f.c), scale*p
+    (vsip_smmul_f.c) and p + gram (vsip_madd_f.c), each a float32 operation
+    rounded once, as the reference's C does."""
+    f32 = np.float32
+    Nsens, Nts = data.col_length, data.row_length
+    d = data.get().astype(f32)
+    d = np.multiply(ts[None, :Nts].astype(f32), d, dtype=f32)
+    d = np.multiply(arr[:Nsens, None].astype(f32), d, dtype=f32)
+    data.set(d)
+    Plan(RCOP, Nsens, Nts, 1.0, FWD, ROW, f32).rcfftmop(data, freq)
+    Plan(CCIP, Nsens, Nts // 2 + 1, 1.0, FWD, COL, f32).ccfftmip(freq)
+    z = freq.get()
+    re, im = z.real.astype(f32), z.imag.astype(f32)
+    p = np.add(np.multiply(re, re, dtype=f32), np.multiply(im, im, dtype=f32), dtype=f32)
+    p = np.multiply(f32(scale), p, dtype=f32)
+    freq.set(p.astype(np.complex64) + 1j * im.astype(np.complex64))
+    gram.set(np.add(p, gram.get().astype(f32), dtype=f32))

@@ -100,6 +100,18 @@ def lib():
                 f = getattr(L, name + s)
                 f.restype = C.c_void_p
                 f.argtypes = [C.c_void_p]
+        # the elementwise calls of the k-omega example (kw.c)
+        L.vsip_vmmul_f.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+        L.vsip_mcmagsq_f.argtypes = [C.c_void_p, C.c_void_p]
+        L.vsip_smmul_f.argtypes = [C.c_float, C.c_void_p, C.c_void_p]
+        L.vsip_madd_f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.vsip_mrealview_f.restype = C.c_void_p
+        L.vsip_mrealview_f.argtypes = [C.c_void_p]
+        L.vsip_vcreate_hanning_f.restype = C.c_void_p
+        L.vsip_vcreate_hanning_f.argtypes = [C.c_ulong, C.c_int]
+        L.vsip_vget_f.restype = C.c_float
+        L.vsip_vget_f.argtypes = [C.c_void_p, C.c_ulong]
+        L.vsip_valldestroy_f.argtypes = [C.c_void_p]
         L.vsip_init(None)
     return _lib
 
@@ -254,3 +266,44 @@ class RefFFT:
 
     def crfftop(self, z, x):
         self._run("crfftop", (z, False), (x, True))
+
+
+def hanning_f(n: int) -> np.ndarray:
+    """The reference's vsip_vcreate_hanning_f(n) values."""
+    L = lib()
+    v = L.vsip_vcreate_hanning_f(n, 0)
+    out = np.array([L.vsip_vget_f(v, i) for i in range(n)], np.float32)
+    L.vsip_valldestroy_f(v)
+    return out
+
+
+def komega_f(ts, arr, data, freq, gram, scale):
+    """kw.c komega() (examples/komegaExamples/kw_c/kw.c:8-26) through the
+    reference library: ts / arr are float32 arrays, data an RView (Nsens x Nts),
+    freq a CView (Nsens x Nts/2+1, interleaved), gram an RView; all updated in
+    place as the reference leaves them."""
+    L = lib()
+    Nsens, Nts = data.col_length, data.row_length
+    Nfreq = Nts // 2 + 1
+    tsb = _Bound(RView(ts, 0, 1, 1, 1, ts.size), True, with_view=False)
+    arb = _Bound(RView(arr, 0, 1, 1, 1, arr.size), True, with_view=False)
+    vts = L.vsip_vbind_f(tsb.blk, 0, 1, Nts)
+    varr = L.vsip_vbind_f(arb.blk, 0, 1, Nsens)
+    xb, fb, gb = _Bound(data, True), _Bound(freq, False), _Bound(gram, True)
+    rc = L.vsip_rcfftmop_create_f(Nsens, Nts, 1.0, 0, 0, 0)
+    cc = L.vsip_ccfftmip_create_f(Nsens, Nfreq, 1.0, -1, 1, 0, 0)
+    L.vsip_vmmul_f(vts, xb.view, 0, xb.view)
+    L.vsip_vmmul_f(varr, xb.view, 1, xb.view)
+    L.vsip_rcfftmop_f(rc, xb.view, fb.view)
+    L.vsip_ccfftmip_f(cc, fb.view)
+    rm = L.vsip_mrealview_f(fb.view)
+    L.vsip_mcmagsq_f(fb.view, rm)
+    L.vsip_smmul_f(scale, rm, rm)
+    L.vsip_madd_f(rm, gb.view, gb.view)
+    L.vsip_mdestroy_f(rm)
+    L.vsip_fftm_destroy_f(rc)
+    L.vsip_fftm_destroy_f(cc)
+    L.vsip_vdestroy_f(vts)
+    L.vsip_vdestroy_f(varr)
+    for b in (tsb, arb, xb, fb, gb):
+        b.close()

@@ -233,3 +233,49 @@ def kat_run(t, plan):
         return y.get()[0]
     plan.crfftop(x, y)
     return y.get()[0].astype(np.complex128)
+
+
+# ------------------------------------------------------------------ k-omega pipeline cases
+_kw_meta = None
+_kw_arrays = None
+
+
+def komega_cases():
+    global _kw_meta
+    if _kw_meta is None:
+        with open(os.path.join(GOLDEN, "komega_cases.json")) as f:
+            _kw_meta = json.load(f)
+    return _kw_meta["cases"]
+
+
+def komega_arrays():
+    global _kw_arrays
+    if _kw_arrays is None:
+        _kw_arrays = dict(np.load(os.path.join(GOLDEN, "komega_cases.npz")))
+    return _kw_arrays
+
+
+def komega_views(c):
+    """Fresh (data, freq, gram, scale) of a k-omega case: data Nsens x Nts rows
+    of pitch `pitch` at offset `doff` (host-exact U[-1,1) stream, seed
+    1000 + seed), freq Nsens x (Nts/2 + 1) interleaved, column-major ("col",
+    as kw.c creates it) or row-major, gram the same shape at offset `goff`
+    holding |U[-1,1)| (seed 2000 + seed)."""
+    Ns, Nt, pitch, doff, goff = c["Nsens"], c["Nts"], c["pitch"], c["doff"], c["goff"]
+    Nf = Nt // 2 + 1
+    data = O.RView(O.fill(doff + Ns * pitch, 1000 + c["seed"], 0, np.float32), doff, pitch, Ns, 1, Nt)
+    fbuf = np.zeros(2 * Ns * Nf, np.float32)
+    freq = O.CView(fbuf, 0, 1, Ns, Ns, Nf) if c["freq"] == "col" else O.CView(fbuf, 0, Nf, Ns, 1, Nf)
+    gbuf = np.abs(O.fill(goff + Ns * Nf, 2000 + c["seed"], 0, np.float32))
+    gram = O.RView(gbuf, goff, 1, Ns, Ns, Nf) if c["gram"] == "col" else O.RView(gbuf, goff, Nf, Ns, 1, Nf)
+    return data, freq, gram, np.float32(c["scale"])
+
+
+def komega_reference(c, name):
+    """(indices, values) of the reference's output block `name` (data_out,
+    freq_out or gram_out) available in the fixture."""
+    A = komega_arrays()
+    k = c["id"] + "__" + name
+    if k in A:
+        return np.arange(A[k].size), A[k]
+    return A[k + "__idx"], A[k + "__val"]
