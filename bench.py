@@ -29,7 +29,9 @@ calls), vec / vecd / vecrc (one single FFT of --points points: c64, c128,
 real f32 -> c64), cols / rows (2^24 c64 points as --points-point transforms
 down the columns / along the rows of a matrix), komega (the k-omega power
 estimate of the reference's kw example on --kw-sensors x --kw-samples real
-data through jvsip_komega_f), measured the same way.
+data through jvsip_komega_f), split (2^24 c64 points as --points-point rows
+of split-complex blocks, real and imaginary parts in separate arrays),
+measured the same way.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload NAME]
 
@@ -54,7 +56,7 @@ sys.path.insert(0, ROOT)
 METRIC = "batched FFT GB/s (% HBM peak): split-TC & batched vs plain FP32 at ≤1e-6 rel err"
 FALLBACK_HBM = 6800.0
 WORKLOADS = ["cfg3", "cfg1", "cfg2col", "cfg2rc", "cfg2cr", "cfg3d", "cfg4", "cfg5", "vec", "vecd", "vecrc", "cols",
-             "rows", "komega"]
+             "rows", "komega", "split"]
 
 
 def args():
@@ -362,6 +364,19 @@ def other_workload(a):
         call = lambda: L.vsip_ccfftmop_f(plan.h, vx.h, vy.h)
         nbytes, dt = 16 * tot, "f32"
         desc = f"vsip_ccfftmop_f {M}x{N} c64 {'VSIP_COL' if w == 'cols' else 'VSIP_ROW'} ({n}-point transforms), N(0,1)"
+    elif w == "split":
+        # 2^24 points as n-point rows of split complex blocks (cstride 1)
+        n, tot = a.points, 1 << 24
+        M, N = tot // n, n
+        xr, xi = synth.fill(tot, 12, 1), synth.fill(tot, 13, 1)
+        x = np.concatenate([xr, xi])
+        y = np.zeros(2 * tot, np.float32)
+        plan = J.FFTM(J.KIND_CCOP, M, N, 1.0, -1, J.VSIP_ROW)
+        bx, by = J.CBlock(xr, xi), J.CBlock(y[:tot], y[tot:])
+        vx, vy = bx.view(0, N, M, 1, N), by.view(0, N, M, 1, N)
+        call = lambda: L.vsip_ccfftmop_f(plan.h, vx.h, vy.h)
+        nbytes, dt = 16 * tot, "f32"
+        desc = f"vsip_ccfftmop_f {M}x{N} c64 VSIP_ROW, split complex blocks (cstride 1), N(0,1)"
     elif w in ("vec", "vecd", "vecrc"):
         # one single FFT of --points points (vsip_ccfftop / vsip_rcfftop)
         N = M = a.points

@@ -165,6 +165,8 @@ constexpr long kLongFewMin = 8192;
 bool launch_smem_f32(const Job &j, cudaStream_t s);
 bool launch_smem_f64(const Job &j, cudaStream_t s);
 bool launch_smem_real_f32(const Job &j, cudaStream_t s);  // R2C / C2R instances
+bool launch_smem_split_f32(const Job &j, cudaStream_t s); // c2c on split complex views (both sides)
+bool launch_smem_split_f64(const Job &j, cudaStream_t s);
 bool launch_komega_r2c_f32(const Job &j, cudaStream_t s); // tapered R2C rows (taper_* set)
 bool launch_komega_power_f32(const Job &j, cudaStream_t s); // c2c columns accumulating power (gram set)
 bool launch_smem_real_f64(const Job &j, cudaStream_t s);

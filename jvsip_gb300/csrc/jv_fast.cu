@@ -1,5 +1,5 @@
 // jv_fast.cu -- register-resident kernels for contiguous rows (single
-// precision, interleaved, unit element stride, any row pitch).
+// precision, interleaved or split complex, unit element stride, any row pitch).
 //
 // A transform of N = R1*R2*...*Rp points is held by T threads, E = N/T
 // complex values each, in registers.  Pass 1 reads global memory directly
@@ -31,6 +31,10 @@ __device__ __forceinline__ int padx(int i) { return i + (i >> 4); }
 struct FastArgs {
     const float2 *in;   // row v starts at in + off_in + v*vs_in
     float2 *out;
+    // split complex views (SPLIT instances): real / imaginary arrays, element
+    // n of row v at [off + v*vs + n]
+    const float *in_re, *in_im;
+    float *out_re, *out_im;
     long off_in, vs_in, off_out, vs_out;
     long nvec;
     int inv;
@@ -79,10 +83,10 @@ __device__ __forceinline__ void store_pass(const float2 (&v)[E], float2 *s, int 
 }
 
 // Passes after the first.  On entry shared memory holds the previous pass's output.
-template <int N, int T, int E, int NsIn, int Off, typename L> struct Passes;
+template <int N, int T, int E, int NsIn, int Off, typename L, bool SPLIT> struct Passes;
 
-template <int N, int T, int E, int NsIn, int Off, int R0, int... Rs>
-struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>> {
+template <int N, int T, int E, int NsIn, int Off, int R0, int... Rs, bool SPLIT>
+struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>, SPLIT> {
     static __device__ __forceinline__ void run(float2 (&v)[E], float2 *s, int t, const FastArgs &a, long row,
                                                bool live) {
         __syncthreads();
@@ -91,7 +95,7 @@ struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>> {
         if constexpr (sizeof...(Rs) == 0) {
             // last pass: j < N/R0 = NsIn, so element j + r*NsIn -- coalesced stores
             if (live) {
-                float2 *o = a.out + a.off_out + row * a.vs_out;
+                const long ob = a.off_out + row * a.vs_out;
                 constexpr int B = E / R0;
 #pragma unroll
                 for (int b = 0; b < B; b++) {
@@ -101,19 +105,24 @@ struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>> {
                         float2 c = v[b * R0 + r];
                         if (a.inv) c.y = -c.y;
                         if (a.has_scale) c = cscale(c, a.scale);
-                        o[j + r * NsIn] = c;
+                        if constexpr (SPLIT) {
+                            a.out_re[ob + j + r * NsIn] = c.x;
+                            a.out_im[ob + j + r * NsIn] = c.y;
+                        } else {
+                            a.out[ob + j + r * NsIn] = c;
+                        }
                     }
                 }
             }
         } else {
             __syncthreads();
             store_pass<N, T, E, R0>(v, s, t, NsIn);
-            Passes<N, T, E, NsIn * R0, Off + R0 * NsIn, RList<Rs...>>::run(v, s, t, a, row, live);
+            Passes<N, T, E, NsIn * R0, Off + R0 * NsIn, RList<Rs...>, SPLIT>::run(v, s, t, a, row, live);
         }
     }
 };
 
-template <int N, int T, int RPC, typename L>
+template <int N, int T, int RPC, typename L, bool SPLIT>
 __global__ void __launch_bounds__(T *RPC) k_fast(const FastArgs pa) {
     constexpr int E = N / T;
     constexpr int R1 = L::first;
@@ -129,26 +138,33 @@ __global__ void __launch_bounds__(T *RPC) k_fast(const FastArgs pa) {
     const bool live = row < a.nvec;
     const long rowc = live ? row : a.nvec - 1;
     float2 v[E];
-    const float2 *in = a.in + a.off_in + rowc * a.vs_in;
+    const long ib = a.off_in + rowc * a.vs_in;
     constexpr int B1 = E / R1;
 #pragma unroll
     for (int b = 0; b < B1; b++)
 #pragma unroll
         for (int r = 0; r < R1; r++) {
-            float2 c = in[t + T * b + r * (N / R1)];
+            const long e = ib + t + T * b + r * (N / R1);
+            float2 c;
+            if constexpr (SPLIT) c = make_float2(a.in_re[e], a.in_im[e]);
+            else c = a.in[e];
             if (a.inv) c.y = -c.y;
             v[b * R1 + r] = c;
         }
     fast_bfly<N, T, R1, E, 1>(v, t, nullptr);
     store_pass<N, T, E, R1>(v, s, t, 1);
-    Passes<N, T, E, R1, R1, typename L::rest>::run(v, s, t, a, rowc, live);
+    Passes<N, T, E, R1, R1, typename L::rest, SPLIT>::run(v, s, t, a, rowc, live);
 }
 
-template <int N, int T, int RPC, typename L>
+template <int N, int T, int RPC, typename L, bool SPLIT>
 static bool launch_fast_n(const Job &j, cudaStream_t st) {
     FastArgs a;
     a.in = (const float2 *)j.cin.re;
     a.out = (float2 *)j.cout.re;
+    a.in_re = (const float *)j.cin.re;
+    a.in_im = (const float *)j.cin.im;
+    a.out_re = (float *)j.cout.re;
+    a.out_im = (float *)j.cout.im;
     a.off_in = j.cin.off;
     a.vs_in = j.cin.vs;
     a.off_out = j.cout.off;
@@ -164,14 +180,14 @@ static bool launch_fast_n(const Job &j, cudaStream_t st) {
     static bool attr = false;
     if (!attr) {
         if (smem > 48 * 1024 &&
-            !cuda_ok(cudaFuncSetAttribute(k_fast<N, T, RPC, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            !cuda_ok(cudaFuncSetAttribute(k_fast<N, T, RPC, L, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)smem),
                      "cudaFuncSetAttribute"))
             return false;
         attr = true;
     }
     long grid = (j.nvec + RPC - 1) / RPC;
-    k_fast<N, T, RPC, L><<<(unsigned)grid, T * RPC, smem, st>>>(a);
+    k_fast<N, T, RPC, L, SPLIT><<<(unsigned)grid, T * RPC, smem, st>>>(a);
     count_launch();
     return cuda_ok(cudaGetLastError(), "k_fast launch");
 }
@@ -191,32 +207,43 @@ std::vector<int> fast_radices(long N) {
     }
 }
 
-// Specialised kernels: contiguous interleaved rows, any pitch, forward or
-// inverse (conjugation folded into load and store), optional scale.
+template <bool SPLIT>
+static bool launch_fast_s(const Job &j, cudaStream_t st) {
+    switch (j.N) {
+        case 64: return launch_fast_n<64, 4, 64, RList<16, 4>, SPLIT>(j, st);
+        case 128: return launch_fast_n<128, 8, 32, RList<16, 8>, SPLIT>(j, st);
+        case 256: return launch_fast_n<256, 16, 16, RList<16, 16>, SPLIT>(j, st);
+        case 512: return launch_fast_n<512, 32, 8, RList<16, 16, 2>, SPLIT>(j, st);
+        case 1024: return launch_fast_n<1024, 64, 4, RList<16, 16, 4>, SPLIT>(j, st);
+        case 2048: return launch_fast_n<2048, 128, 2, RList<16, 16, 8>, SPLIT>(j, st);
+        case 4096: return launch_fast_n<4096, 256, 1, RList<16, 16, 16>, SPLIT>(j, st);
+        case 8192: return launch_fast_n<8192, 512, 1, RList<16, 16, 16, 2>, SPLIT>(j, st);
+        default: return false;
+    }
+}
+
+// Specialised kernels: contiguous rows, interleaved or split complex (both
+// views alike), any pitch, forward or inverse (conjugation folded into load
+// and store), optional scale.
 bool launch_fast_f32(const Job &j, cudaStream_t st) {
     if (j.no_fast) return false;
     if (j.kind != K_C2C || j.prec != P_F32) return false;
     const CView &ci = j.cin, &co = j.cout;
-    // interleaved, unit element stride, 8-byte aligned, rows of the transform contiguous
-    if (ci.cst != 2 || co.cst != 2 || ci.es != 1 || co.es != 1) return false;
-    if ((const float *)ci.im != (const float *)ci.re + 1 || (const float *)co.im != (const float *)co.re + 1)
-        return false;
-    if (((uintptr_t)ci.re % 8) || ((uintptr_t)co.re % 8)) return false;
+    if (ci.es != 1 || co.es != 1) return false;
+    // split complex: separate real and imaginary arrays on both sides
+    const bool split = ci.cst == 1 && co.cst == 1;
+    if (!split) {
+        // interleaved, 8-byte aligned
+        if (ci.cst != 2 || co.cst != 2) return false;
+        if ((const float *)ci.im != (const float *)ci.re + 1 || (const float *)co.im != (const float *)co.re + 1)
+            return false;
+        if (((uintptr_t)ci.re % 8) || ((uintptr_t)co.re % 8)) return false;
+    }
     if (j.nvec <= 0 || j.nvec > 0x7fffffffL * 1L) return false;
     // rows of an in-place call must not overlap each other (each CTA reads its
     // rows completely before it writes them)
     if (j.nvec > 1 && (labs(ci.vs) < j.N || labs(co.vs) < j.N)) return false;
-    switch (j.N) {
-        case 64: return launch_fast_n<64, 4, 64, RList<16, 4>>(j, st);
-        case 128: return launch_fast_n<128, 8, 32, RList<16, 8>>(j, st);
-        case 256: return launch_fast_n<256, 16, 16, RList<16, 16>>(j, st);
-        case 512: return launch_fast_n<512, 32, 8, RList<16, 16, 2>>(j, st);
-        case 1024: return launch_fast_n<1024, 64, 4, RList<16, 16, 4>>(j, st);
-        case 2048: return launch_fast_n<2048, 128, 2, RList<16, 16, 8>>(j, st);
-        case 4096: return launch_fast_n<4096, 256, 1, RList<16, 16, 16>>(j, st);
-        case 8192: return launch_fast_n<8192, 512, 1, RList<16, 16, 16, 2>>(j, st);
-        default: return false;
-    }
+    return split ? launch_fast_s<true>(j, st) : launch_fast_s<false>(j, st);
 }
 
 }  // namespace jv

@@ -6,6 +6,7 @@
 
 namespace jv {
 bool launch_smem_f32(const Job &j, cudaStream_t s) {
+    if (j.kind == K_C2C && j.cin.cst == 1 && j.cout.cst == 1) return launch_smem_split_f32(j, s);
     if (j.kind == K_C2C) return launch_smem_t<float, K_C2C>(j, s);
     return launch_smem_real_f32(j, s);
 }

@@ -6,6 +6,7 @@
 
 namespace jv {
 bool launch_smem_f64(const Job &j, cudaStream_t s) {
+    if (j.kind == K_C2C && j.cin.cst == 1 && j.cout.cst == 1) return launch_smem_split_f64(j, s);
     if (j.kind == K_C2C) return launch_smem_t<double, K_C2C>(j, s);
     return launch_smem_real_f64(j, s);
 }

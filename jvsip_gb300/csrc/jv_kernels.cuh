@@ -590,11 +590,31 @@ template <typename T> struct TileIO {
     T *gram;
     long g_es, g_vs;
     T g_scale;
+    // split complex views (FX_SPLIT): element (t, n) at in_re / in_im
+    // [t*in_vs + n*in_es], out_re / out_im [t*out_vs + n*out_es]
+    const T *in_re, *in_im;
+    T *out_re, *out_im;
 };
 
 // FX flags of the fused passes
 constexpr int FX_TAPER = 1;  // first pass: taper the loaded real pairs, optionally write them back
 constexpr int FX_POWER = 2;  // last pass: store (s|X|^2, Im X), gram += s|X|^2
+constexpr int FX_SPLIT = 4;  // split complex views: real and imaginary parts in separate arrays
+
+template <int FX, typename C, typename T>
+__device__ __forceinline__ C io_load(const TileIO<T> &io, const C *src, long e) {
+    if constexpr ((FX & FX_SPLIT) != 0) return mk<C>(io.in_re[e], io.in_im[e]);
+    else return src[e];
+}
+template <int FX, typename C, typename T>
+__device__ __forceinline__ void io_store(const TileIO<T> &io, C *dst, long e, C v) {
+    if constexpr ((FX & FX_SPLIT) != 0) {
+        io.out_re[e] = v.x;
+        io.out_im[e] = v.y;
+    } else {
+        dst[e] = v;
+    }
+}
 
 // the tapered pair at complex index n of transform t: x_2n*tp_n[2n] then
 // *tp_t[t] (c_VSIP_src/vsip_vmmul_f.c: rows by the time taper, then columns by
@@ -652,11 +672,11 @@ __device__ __forceinline__ void pass_first(typename cplx_t<T>::t *s, int ld, int
         if (b < nb) {
             int t, j;
             tile_tj(b, io.vf, nt, io.mnt, NR, pc.y, t, j);
-            const C *src = io.in + ((long)t * io.in_vs + (long)j * io.in_es);
+            const long e0 = (long)t * io.in_vs + (long)j * io.in_es;
             const long st = (long)NR * io.in_es;
 #pragma unroll
             for (int r = 0; r < R; r++) {
-                C c = src[r * st];
+                C c = io_load<FX>(io, io.in, e0 + r * st);
                 if constexpr ((FX & FX_TAPER) != 0) {
                     c = taper_pair(c, io, (long)(j + r * NR), t);
                     if (io.wb) io.wb[(long)t * io.in_vs + (long)(j + r * NR) * io.in_es] = c;
@@ -675,12 +695,11 @@ __device__ __forceinline__ void pass_first(typename cplx_t<T>::t *s, int ld, int
             Dft<C, R>::run(v[k]);
             if (LAST) {
                 // one pass: N = R, j = 0, output element r
-                C *dst = io.out + (long)t * io.out_vs;
 #pragma unroll
                 for (int r = 0; r < R; r++) {
                     C o = out_value(v[k][r], io.smask_out, io.has_scale, io.scale);
                     if constexpr ((FX & FX_POWER) != 0) o = power_out(o, io, (long)t, (long)r);
-                    dst[r * io.out_es] = o;
+                    io_store<FX>(io, io.out, (long)t * io.out_vs + r * io.out_es, o);
                 }
             } else {
                 C *dst = s + t * ld;
@@ -732,13 +751,13 @@ __device__ __forceinline__ void pass_last(const typename cplx_t<T>::t *s, int ld
                     v[k][r] = cmul(v[k][r], tw_two_level(io.tw_lo, io.tw_hi, io.tw_mask, io.tw_sh,
                                                          tg * (unsigned)(j + r * Ns)));
             }
-            C *dst = io.out + ((long)t * io.out_vs + (long)j * io.out_es);
+            const long e0 = (long)t * io.out_vs + (long)j * io.out_es;
             const long st = (long)Ns * io.out_es;
 #pragma unroll
             for (int r = 0; r < R; r++) {
                 C o = out_value(v[k][r], io.smask_out, io.has_scale, io.scale);
                 if constexpr ((FX & FX_POWER) != 0) o = power_out(o, io, (long)t, (long)(j + r * Ns));
-                dst[r * st] = o;
+                io_store<FX>(io, io.out, e0 + r * st, o);
             }
         }
     }
@@ -920,13 +939,17 @@ __device__ __forceinline__ void tile_load(Walk &w, bool vf, int tot, C *s, int l
 
 // Instances of the shared-memory kernel beyond the three transform kinds:
 // the k-omega pipeline's tapered R2C rows and power-accumulating c2c columns.
-constexpr int KX_R2C_TAPER = 3, KX_C2C_POWER = 4;
+constexpr int KX_R2C_TAPER = 3, KX_C2C_POWER = 4, KX_C2C_SPLIT = 5;
 
 template <typename T, int KIND0, int EMAX, int MAXT>
 __global__ void __launch_bounds__(MAXT) k_smem(const __grid_constant__ SmemArgs<T> a) {
     typedef typename cplx_t<T>::t C;
-    constexpr int KIND = KIND0 == KX_R2C_TAPER ? K_R2C : KIND0 == KX_C2C_POWER ? K_C2C : KIND0;
-    constexpr int FX = KIND0 == KX_R2C_TAPER ? FX_TAPER : KIND0 == KX_C2C_POWER ? FX_POWER : 0;
+    constexpr int KIND =
+        KIND0 == KX_R2C_TAPER ? K_R2C : (KIND0 == KX_C2C_POWER || KIND0 == KX_C2C_SPLIT) ? K_C2C : KIND0;
+    constexpr int FX = KIND0 == KX_R2C_TAPER   ? FX_TAPER
+                       : KIND0 == KX_C2C_POWER ? FX_POWER
+                       : KIND0 == KX_C2C_SPLIT ? FX_SPLIT
+                                               : 0;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     C *s = reinterpret_cast<C *>(smem_raw);
     const int N = a.N, ld = a.ld;
@@ -945,7 +968,9 @@ __global__ void __launch_bounds__(MAXT) k_smem(const __grid_constant__ SmemArgs<
         if (g >= ngroups) return;
         const long v0 = g * a.vpb;
         const int nt = (int)min((long)a.vpb, a.nvec - v0);
-        if (KIND == K_C2C && a.passes != 0 && cin.vec && cout.vec) {
+        constexpr bool SPLIT = (FX & FX_SPLIT) != 0;
+        if (KIND == K_C2C && a.passes != 0 &&
+            (SPLIT ? (cin.cst == 1 && cout.cst == 1) : (cin.vec && cout.vec))) {
             // c2c on interleaved views: first pass from the view, last pass to the view
             TileIO<T> io;
             io.smask_in = a.conj_in ? 0x80000000u : 0u;
@@ -997,8 +1022,18 @@ __global__ void __launch_bounds__(MAXT) k_smem(const __grid_constant__ SmemArgs<
                 staged_tile<T, EMAX, FX>(s, ld, nt, a.vpb, a.passes, a.twg, a.pc, io);
                 return;
             }
-            io.in = reinterpret_cast<const C *>(cin.re) + (cin.off + v0 * cin.vs + by * a.bvs_in);
-            io.out = reinterpret_cast<C *>(cout.re) + (cout.off + v0 * cout.vs + by * a.bvs_out);
+            if constexpr (SPLIT) {
+                const long ei = cin.off + v0 * cin.vs + by * a.bvs_in, eo = cout.off + v0 * cout.vs + by * a.bvs_out;
+                io.in_re = cin.re + ei;
+                io.in_im = cin.im + ei;
+                io.out_re = cout.re + eo;
+                io.out_im = cout.im + eo;
+                io.in = nullptr;
+                io.out = nullptr;
+            } else {
+                io.in = reinterpret_cast<const C *>(cin.re) + (cin.off + v0 * cin.vs + by * a.bvs_in);
+                io.out = reinterpret_cast<C *>(cout.re) + (cout.off + v0 * cout.vs + by * a.bvs_out);
+            }
             io.in_es = cin.es;
             io.in_vs = cin.vs;
             io.out_es = cout.es;

@@ -316,6 +316,10 @@ bool launch_smem_t(const Job &j, cudaStream_t st) {
         set_error(E_UNSUPPORTED, "tapered R2C needs real rows of unit stride, even offset and pitch");
         return false;
     }
+    if (KIND == KX_C2C_SPLIT && !(a.cin.cst == 1 && a.cout.cst == 1)) {
+        set_error(E_UNSUPPORTED, "split instance on interleaved views");
+        return false;
+    }
     if (KIND == KX_C2C_POWER && !(a.cin.vec && a.cout.vec)) {
         set_error(E_UNSUPPORTED, "power columns need an interleaved spectrum");
         return false;
