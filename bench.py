@@ -426,11 +426,14 @@ def other_workload(a):
     ms = statistics.mean(per)
     extra = {"config": {"workload": desc, "bytes_per_step": nbytes,
                         "l2": "flushed between calls" if flush is not None else "inputs larger than L2"}}
-    outs = {"": y.copy() if w == "cfg4" else y}
-    if w == "cfg4":
+    outs = {"": y.copy() if w in ("cfg4", "cfg3d") else y}
+    if w in ("cfg4", "cfg3d"):
         # the precision forms on the same plan and data: tensor-core DFT products
+        # (cfg4), double-float arithmetic on the FP32 pipes (cfg3d)
         forms = {}
-        for name, form in (("split_fp16", J.JVSIP_FORM_SPLIT_FP16), ("split_bf16", J.JVSIP_FORM_SPLIT_BF16)):
+        flist = ((("split_fp16", J.JVSIP_FORM_SPLIT_FP16), ("split_bf16", J.JVSIP_FORM_SPLIT_BF16)) if w == "cfg4"
+                 else (("df64", J.JVSIP_FORM_DF64),))
+        for name, form in flist:
             plan.setform(form)
             for _ in range(a.warmup):
                 call()
@@ -443,6 +446,9 @@ def other_workload(a):
             msf = statistics.mean(per_f)
             forms[name] = {"value": round(nbytes / (msf / 1e3) / 1e9, 2), "unit": "GB/s", "ms_per_step": round(msf, 4),
                            "gpu_launches": int(kl)}
+            if w == "cfg3d":
+                ref = outs[""]
+                forms[name]["rel_l2_vs_plain_fp64"] = float(np.linalg.norm(y - ref) / np.linalg.norm(ref))
         plan.setform(J.JVSIP_FORM_PLAIN)
         extra["forms"] = forms
         y = outs[""]

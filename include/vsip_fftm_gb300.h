@@ -344,6 +344,17 @@ int jvsip_blocksync_d(vsip_block_d *b);
 int jvsip_fftm_setform_f(vsip_fftm_f *plan, int form);
 int jvsip_fftm_getform_f(const vsip_fftm_f *plan);
 
+/* FP64 form of a c2c _d plan of 64..8192 points (powers of two): contiguous
+ * interleaved rows are transformed in double-float arithmetic (hi + lo
+ * floats, 48 significant bits, each row shifted by a power of two so its
+ * largest element lies in [1, 2)) on the FP32 pipes instead of the much
+ * slower FP64 pipe; results agree with the plain form to about 1e-14
+ * relative.  Other views and lengths keep the plain form.  Returns 0, or
+ * JVSIP's error code (5: the plan's length or kind has no FP64 form). */
+#define JVSIP_FORM_DF64        4
+int jvsip_fftm_setform_d(vsip_fftm_d *plan, int form);
+int jvsip_fftm_getform_d(const vsip_fftm_d *plan);
+
 /* Batching form: run n independent c2c fftm calls (each plan with its own
  * input/output views; ccfftmop or ccfftmip plans) as one persistent launch fed
  * by a device work queue of (plan, row-tile) descriptors.  Equivalent to

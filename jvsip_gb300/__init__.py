@@ -26,6 +26,7 @@ VSIP_FFT_FWD, VSIP_FFT_INV = -1, 1
 VSIP_MEM_NONE = 0
 VSIP_ALG_SPACE, VSIP_ALG_TIME, VSIP_ALG_NOISE = 0, 1, 2
 JVSIP_FORM_AUTO, JVSIP_FORM_PLAIN, JVSIP_FORM_SPLIT_BF16, JVSIP_FORM_SPLIT_FP16 = 0, 1, 2, 3
+JVSIP_FORM_DF64 = 4
 
 # every symbol include/vsip_fftm_gb300.h declares
 EXPORTS = [
@@ -61,7 +62,7 @@ EXPORTS = [
     "vsip_cvcreate_f", "vsip_cvcreate_d", "vsip_vcreate_f", "vsip_vcreate_d",
     "vsip_cvdestroy_f", "vsip_cvdestroy_d", "vsip_vdestroy_f", "vsip_vdestroy_d",
     "vsip_cvalldestroy_f", "vsip_cvalldestroy_d", "vsip_valldestroy_f", "vsip_valldestroy_d",
-    "jvsip_komega_f",
+    "jvsip_komega_f", "jvsip_fftm_setform_d", "jvsip_fftm_getform_d",
 ]
 
 
@@ -193,6 +194,8 @@ def lib(load_only: bool = False):
     L.jvsip_fftm_autotune_entries.restype = C.c_long
     L.jvsip_fftm_setform_f.argtypes = [vp, C.c_int]
     L.jvsip_fftm_getform_f.argtypes = [vp]
+    L.jvsip_fftm_setform_d.argtypes = [vp, C.c_int]
+    L.jvsip_fftm_getform_d.argtypes = [vp]
     L.jvsip_fftm_batch_f.argtypes = [C.c_size_t, vp, vp, vp]
     L.jvsip_fftm_batch_create_f.restype = vp
     L.jvsip_fftm_batch_create_f.argtypes = [C.c_size_t, vp, vp, vp]
@@ -382,9 +385,9 @@ class FFTM:
         return a
 
     def setform(self, form: int):
-        rc = lib().jvsip_fftm_setform_f(self.h, form)
+        rc = getattr(lib(), "jvsip_fftm_setform" + self.s)(self.h, form)
         if rc:
-            raise RuntimeError("jvsip_fftm_setform_f failed: %d" % rc)
+            raise RuntimeError("jvsip_fftm_setform%s failed: %d" % (self.s, rc))
 
     def passes(self):
         buf = (C.c_int * 40)()

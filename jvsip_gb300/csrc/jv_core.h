@@ -103,6 +103,7 @@ struct Job {
     const void *twp = nullptr;    // per-pass twiddle tables of the specialised kernel (or null)
     const void *twg = nullptr;    // per-pass twiddle tables of the general kernel's schedule
     const void *pc = nullptr;     // per-pass constants of that schedule (PassConst)
+    const void *twdd = nullptr;   // per-pass double-float twiddles of the FP64 form (or null)
     int npass = 0;
     int radix[40];
     int form = 0;        // JVSIP_FORM_* of the plan
@@ -175,6 +176,8 @@ bool launch_global_f64(const Job &j, cudaStream_t s);
 bool launch_fast_f32(const Job &j, cudaStream_t s);   // specialised kernels; false when none fits
 std::vector<int> fast_radices(long N);                // radix list of the specialised kernel for N
 bool launch_split_f32(const Job &j, cudaStream_t s);  // precision form; false when the call does not qualify
+bool launch_fast_dd(const Job &j, cudaStream_t s);    // FP64 form (double-float rows); false when it does not qualify
+std::vector<int> dd_radices(long N);                  // radix list of the FP64 form for N (empty: none)
 int split_status_check(cudaStream_t s);               // device status of the precision form (0 = clean)
 // real long transforms: in-place Hermitian split of Z on an interleaved view,
 // C2R un-split into dense conjugated Y, and the final store of dense conjugated y
@@ -213,6 +216,7 @@ struct Plan {
     void *d_twp = nullptr;    // per-pass [r][m] twiddle tables of the specialised kernel
     void *d_twg = nullptr;    // per-pass [r][m] twiddle tables of the general kernel's schedule
     void *d_pc = nullptr;     // per-pass constants of that schedule (PassConst, one per pass)
+    void *d_twdd = nullptr;   // per-pass double-float tables of the FP64 form (built by setform_d)
     std::vector<unsigned long> jofk;  // reference digit-reversal map (kept for parity checks)
     std::vector<CallGraph> graphs;    // captured calls (ntimes == 0), most recent last
     bool single = false;      // a single-FFT plan (vsip_fft_*: one row, vector views)

@@ -441,6 +441,9 @@ static bool run_job(Job &j, cudaStream_t st) {
     if (j.form == JVSIP_FORM_SPLIT_BF16 || j.form == JVSIP_FORM_SPLIT_FP16) {
         if (launch_split_f32(j, st)) return jvsip_gpu_last_error() == 0;
     }
+    if (j.form == JVSIP_FORM_DF64 && j.twdd) {
+        if (launch_fast_dd(j, st)) return jvsip_gpu_last_error() == 0;
+    }
     // few transforms of a length with a decomposition: two steps over many
     // CTAs instead of one CTA per transform
     const bool few = j.lp && j.nvec * 2 < (long)device()->sms && j.N >= kLongFewMin;
@@ -569,6 +572,7 @@ static void fill_job(Job &j, const Plan *p, int kind) {
     j.twp = p->d_twp;
     j.twg = p->d_twg;
     j.pc = p->d_pc;
+    j.twdd = p->d_twdd;
     j.form = p->form;
     j.no_fast = p->no_fast;
     j.no_pipeline = p->no_pipeline;

@@ -432,6 +432,7 @@ static void plan_free(Plan *p) {
         if (g.exec) cudaGraphExecDestroy(g.exec);
     long_free(p->lp);
     release_tables(p);
+    dfree(p->d_twdd);
     delete p;
 }
 
@@ -748,6 +749,50 @@ int jvsip_fftm_setform_f(vsip_fftm_f *vp, int form) {
     return 0;
 }
 int jvsip_fftm_getform_f(const vsip_fftm_f *vp) {
+    Plan *p = plan_of(vp);
+    return p ? p->form : -1;
+}
+
+// The FP64 form of a c2c _d plan: double-float twiddles of its radix-8/4/2
+// schedule, [r][m] per pass as in the single-precision tables.
+int jvsip_fftm_setform_d(vsip_fftm_d *vp, int form) {
+    Plan *p = plan_of(vp);
+    if (!p || (form != JVSIP_FORM_AUTO && form != JVSIP_FORM_PLAIN && form != JVSIP_FORM_DF64)) return E_ARG;
+    std::lock_guard<std::mutex> lk(p->mu);
+    if (form == JVSIP_FORM_DF64 && !p->d_twdd) {
+        const std::vector<int> rad = dd_radices(p->MN);
+        if (rad.empty() || (p->type != JV_CCFFTOP && p->type != JV_CCFFTIP)) {
+            set_error(E_UNSUPPORTED, "the FP64 form takes c2c plans of 64 to 8192 points (powers of two)");
+            return E_UNSUPPORTED;
+        }
+        std::vector<float> tb;
+        long Ns = 1;
+        for (int R : rad) {
+            for (long r = 0; r < R; r++)
+                for (long m = 0; m < Ns; m++) {
+                    double c, sn;
+                    unit_root((r * m) % (Ns * R), Ns * R, &c, &sn);
+                    for (double x : {c, sn}) {
+                        const float hi = (float)x;
+                        tb.push_back(hi);
+                        tb.push_back((float)(x - (double)hi));
+                    }
+                }
+            Ns *= R;
+        }
+        void *d = dmalloc(tb.size() * sizeof(float));
+        if (!d) return E_ALLOC;
+        if (!cuda_ok(cudaMemcpy(d, tb.data(), tb.size() * sizeof(float), cudaMemcpyHostToDevice),
+                     "FP64-form twiddle upload")) {
+            dfree(d);
+            return E_CUDA;
+        }
+        p->d_twdd = d;
+    }
+    p->form = form;
+    return 0;
+}
+int jvsip_fftm_getform_d(const vsip_fftm_d *vp) {
     Plan *p = plan_of(vp);
     return p ? p->form : -1;
 }
