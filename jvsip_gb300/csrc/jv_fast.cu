@@ -1,5 +1,6 @@
-// jv_fast.cu -- register-resident kernels for contiguous rows (single
-// precision, interleaved or split complex, unit element stride, any row pitch).
+// jv_fast.cu -- register-resident kernels (single precision, interleaved or
+// split complex) for rows of unit element stride and any pitch, and for
+// column tiles (adjacent transforms of any element stride).
 //
 // A transform of N = R1*R2*...*Rp points is held by T threads, E = N/T
 // complex values each, in registers.  Pass 1 reads global memory directly
@@ -29,8 +30,9 @@ template <> struct RList<> {};
 __device__ __forceinline__ int padx(int i) { return i + (i >> 4); }
 
 struct FastArgs {
-    const float2 *in;   // row v starts at in + off_in + v*vs_in
+    const float2 *in;   // transform v starts at in + off_in + v*vs_in, element n at + n*es_in
     float2 *out;
+    long es_in, es_out; // element strides (1 for rows; the row pitch for column tiles)
     // split complex views (SPLIT instances): real / imaginary arrays, element
     // n of row v at [off + v*vs + n]
     const float *in_re, *in_im;
@@ -83,10 +85,10 @@ __device__ __forceinline__ void store_pass(const float2 (&v)[E], float2 *s, int 
 }
 
 // Passes after the first.  On entry shared memory holds the previous pass's output.
-template <int N, int T, int E, int NsIn, int Off, typename L, bool SPLIT> struct Passes;
+template <int N, int T, int E, int NsIn, int Off, typename L, bool SPLIT, bool COLS> struct Passes;
 
-template <int N, int T, int E, int NsIn, int Off, int R0, int... Rs, bool SPLIT>
-struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>, SPLIT> {
+template <int N, int T, int E, int NsIn, int Off, int R0, int... Rs, bool SPLIT, bool COLS>
+struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>, SPLIT, COLS> {
     static __device__ __forceinline__ void run(float2 (&v)[E], float2 *s, int t, const FastArgs &a, long row,
                                                bool live) {
         __syncthreads();
@@ -105,11 +107,12 @@ struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>, SPLIT> {
                         float2 c = v[b * R0 + r];
                         if (a.inv) c.y = -c.y;
                         if (a.has_scale) c = cscale(c, a.scale);
+                        const long e = ob + (long)(j + r * NsIn) * (COLS ? a.es_out : 1L);
                         if constexpr (SPLIT) {
-                            a.out_re[ob + j + r * NsIn] = c.x;
-                            a.out_im[ob + j + r * NsIn] = c.y;
+                            a.out_re[e] = c.x;
+                            a.out_im[e] = c.y;
                         } else {
-                            a.out[ob + j + r * NsIn] = c;
+                            a.out[e] = c;
                         }
                     }
                 }
@@ -117,20 +120,26 @@ struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>, SPLIT> {
         } else {
             __syncthreads();
             store_pass<N, T, E, R0>(v, s, t, NsIn);
-            Passes<N, T, E, NsIn * R0, Off + R0 * NsIn, RList<Rs...>, SPLIT>::run(v, s, t, a, row, live);
+            Passes<N, T, E, NsIn * R0, Off + R0 * NsIn, RList<Rs...>, SPLIT, COLS>::run(v, s, t, a, row, live);
         }
     }
 };
 
-template <int N, int T, int RPC, typename L, bool SPLIT>
+// Rows (COLS false): RPC transforms per CTA, T consecutive threads per
+// transform.  Column tiles (COLS true): RPC adjacent transforms per CTA with
+// consecutive threads on adjacent transforms, so every load and store of a
+// warp covers RPC neighbouring elements of each row it touches; each
+// transform's shared-memory row has an odd pitch so the RPC rows fall in
+// different banks.
+template <int N, int T, int RPC, typename L, bool SPLIT, bool COLS>
 __global__ void __launch_bounds__(T *RPC) k_fast(const FastArgs pa) {
     constexpr int E = N / T;
     constexpr int R1 = L::first;
-    constexpr int NP = N + N / 16;  // padded row in shared memory
+    constexpr int NP = N + N / 16 + (COLS ? 1 : 0);  // padded row in shared memory
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const FastArgs a = pa;
-    const int t = threadIdx.x % T;
-    const int rl = threadIdx.x / T;
+    const int t = COLS ? (int)threadIdx.x / RPC : (int)threadIdx.x % T;
+    const int rl = COLS ? (int)threadIdx.x % RPC : (int)threadIdx.x / T;
     const long row = (long)blockIdx.x * RPC + rl;
     float2 *s = reinterpret_cast<float2 *>(smem_raw) + rl * NP;
     // rows past the end (last CTA only) recompute the last row and store nothing,
@@ -144,7 +153,7 @@ __global__ void __launch_bounds__(T *RPC) k_fast(const FastArgs pa) {
     for (int b = 0; b < B1; b++)
 #pragma unroll
         for (int r = 0; r < R1; r++) {
-            const long e = ib + t + T * b + r * (N / R1);
+            const long e = ib + (long)(t + T * b + r * (N / R1)) * (COLS ? a.es_in : 1L);
             float2 c;
             if constexpr (SPLIT) c = make_float2(a.in_re[e], a.in_im[e]);
             else c = a.in[e];
@@ -153,14 +162,16 @@ __global__ void __launch_bounds__(T *RPC) k_fast(const FastArgs pa) {
         }
     fast_bfly<N, T, R1, E, 1>(v, t, nullptr);
     store_pass<N, T, E, R1>(v, s, t, 1);
-    Passes<N, T, E, R1, R1, typename L::rest, SPLIT>::run(v, s, t, a, rowc, live);
+    Passes<N, T, E, R1, R1, typename L::rest, SPLIT, COLS>::run(v, s, t, a, rowc, live);
 }
 
-template <int N, int T, int RPC, typename L, bool SPLIT>
+template <int N, int T, int RPC, typename L, bool SPLIT, bool COLS>
 static bool launch_fast_n(const Job &j, cudaStream_t st) {
     FastArgs a;
     a.in = (const float2 *)j.cin.re;
     a.out = (float2 *)j.cout.re;
+    a.es_in = j.cin.es;
+    a.es_out = j.cout.es;
     a.in_re = (const float *)j.cin.re;
     a.in_im = (const float *)j.cin.im;
     a.out_re = (float *)j.cout.re;
@@ -175,19 +186,19 @@ static bool launch_fast_n(const Job &j, cudaStream_t st) {
     a.scale = (float)j.scale;
     a.twp = (const float2 *)j.twp;
     if (!a.twp) return false;
-    constexpr int NP = N + N / 16;
+    constexpr int NP = N + N / 16 + (COLS ? 1 : 0);
     size_t smem = (size_t)RPC * NP * sizeof(float2);
     static bool attr = false;
     if (!attr) {
         if (smem > 48 * 1024 &&
-            !cuda_ok(cudaFuncSetAttribute(k_fast<N, T, RPC, L, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem),
+            !cuda_ok(cudaFuncSetAttribute(k_fast<N, T, RPC, L, SPLIT, COLS>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                      "cudaFuncSetAttribute"))
             return false;
         attr = true;
     }
     long grid = (j.nvec + RPC - 1) / RPC;
-    k_fast<N, T, RPC, L, SPLIT><<<(unsigned)grid, T * RPC, smem, st>>>(a);
+    k_fast<N, T, RPC, L, SPLIT, COLS><<<(unsigned)grid, T * RPC, smem, st>>>(a);
     count_launch();
     return cuda_ok(cudaGetLastError(), "k_fast launch");
 }
@@ -199,6 +210,7 @@ std::vector<int> fast_radices(long N) {
         case 128: return {16, 8};
         case 256: return {16, 16};
         case 512: return {16, 16, 2};
+        case 1000: return {10, 10, 10};
         case 1024: return {16, 16, 4};
         case 2048: return {16, 16, 8};
         case 4096: return {16, 16, 16};
@@ -207,29 +219,53 @@ std::vector<int> fast_radices(long N) {
     }
 }
 
+// Rows: T threads per transform, RPC transforms per CTA.
 template <bool SPLIT>
-static bool launch_fast_s(const Job &j, cudaStream_t st) {
+static bool launch_fast_rows(const Job &j, cudaStream_t st) {
     switch (j.N) {
-        case 64: return launch_fast_n<64, 4, 64, RList<16, 4>, SPLIT>(j, st);
-        case 128: return launch_fast_n<128, 8, 32, RList<16, 8>, SPLIT>(j, st);
-        case 256: return launch_fast_n<256, 16, 16, RList<16, 16>, SPLIT>(j, st);
-        case 512: return launch_fast_n<512, 32, 8, RList<16, 16, 2>, SPLIT>(j, st);
-        case 1024: return launch_fast_n<1024, 64, 4, RList<16, 16, 4>, SPLIT>(j, st);
-        case 2048: return launch_fast_n<2048, 128, 2, RList<16, 16, 8>, SPLIT>(j, st);
-        case 4096: return launch_fast_n<4096, 256, 1, RList<16, 16, 16>, SPLIT>(j, st);
-        case 8192: return launch_fast_n<8192, 512, 1, RList<16, 16, 16, 2>, SPLIT>(j, st);
+        case 64: return launch_fast_n<64, 4, 64, RList<16, 4>, SPLIT, false>(j, st);
+        case 128: return launch_fast_n<128, 8, 32, RList<16, 8>, SPLIT, false>(j, st);
+        case 256: return launch_fast_n<256, 16, 16, RList<16, 16>, SPLIT, false>(j, st);
+        case 512: return launch_fast_n<512, 32, 8, RList<16, 16, 2>, SPLIT, false>(j, st);
+        case 1000: return launch_fast_n<1000, 100, 4, RList<10, 10, 10>, SPLIT, false>(j, st);
+        case 1024: return launch_fast_n<1024, 64, 4, RList<16, 16, 4>, SPLIT, false>(j, st);
+        case 2048: return launch_fast_n<2048, 128, 2, RList<16, 16, 8>, SPLIT, false>(j, st);
+        case 4096: return launch_fast_n<4096, 256, 1, RList<16, 16, 16>, SPLIT, false>(j, st);
+        case 8192: return launch_fast_n<8192, 512, 1, RList<16, 16, 16, 2>, SPLIT, false>(j, st);
         default: return false;
     }
 }
 
-// Specialised kernels: contiguous rows, interleaved or split complex (both
-// views alike), any pitch, forward or inverse (conjugation folded into load
-// and store), optional scale.
+// Column tiles: V adjacent transforms per CTA (V * 8 bytes of each row per
+// warp access), shared memory about 70 KB per CTA for the long ones.
+// Measured on 2^24 points (GB/s, against the shared-memory kernel's column
+// tiles): 64 points 5624 (3664), 256: 5377 (4088), 512: 3478 (2220), 1024:
+// 2927 (2472), 2048: 2059 (2000), 1000 x 4096: 2054 (1785).
+template <bool SPLIT>
+static bool launch_fast_cols(const Job &j, cudaStream_t st) {
+    switch (j.N) {
+        case 64: return launch_fast_n<64, 4, 64, RList<16, 4>, SPLIT, true>(j, st);
+        case 128: return launch_fast_n<128, 8, 32, RList<16, 8>, SPLIT, true>(j, st);
+        case 256: return launch_fast_n<256, 16, 16, RList<16, 16>, SPLIT, true>(j, st);
+        case 512: return launch_fast_n<512, 32, 16, RList<16, 16, 2>, SPLIT, true>(j, st);
+        case 1000: return launch_fast_n<1000, 100, 8, RList<10, 10, 10>, SPLIT, true>(j, st);
+        case 1024: return launch_fast_n<1024, 64, 8, RList<16, 16, 4>, SPLIT, true>(j, st);
+        case 2048: return launch_fast_n<2048, 128, 4, RList<16, 16, 8>, SPLIT, true>(j, st);
+        // 4096 points: two columns per CTA measured slower (1689 GB/s) than the
+        // shared-memory kernel's four (1841 GB/s); it keeps those
+        default: return false;
+    }
+}
+
+// Specialised kernels: rows of unit element stride, or column tiles
+// (adjacent transforms, any element stride), interleaved or split complex
+// (both views alike), forward or inverse (conjugation folded into load and
+// store), optional scale.
 bool launch_fast_f32(const Job &j, cudaStream_t st) {
     if (j.no_fast) return false;
     if (j.kind != K_C2C || j.prec != P_F32) return false;
+    if (j.lp || j.nbatch > 1 || j.tw_lo || j.gram || j.taper_n) return false;
     const CView &ci = j.cin, &co = j.cout;
-    if (ci.es != 1 || co.es != 1) return false;
     // split complex: separate real and imaginary arrays on both sides
     const bool split = ci.cst == 1 && co.cst == 1;
     if (!split) {
@@ -240,10 +276,21 @@ bool launch_fast_f32(const Job &j, cudaStream_t st) {
         if (((uintptr_t)ci.re % 8) || ((uintptr_t)co.re % 8)) return false;
     }
     if (j.nvec <= 0 || j.nvec > 0x7fffffffL * 1L) return false;
-    // rows of an in-place call must not overlap each other (each CTA reads its
-    // rows completely before it writes them)
-    if (j.nvec > 1 && (labs(ci.vs) < j.N || labs(co.vs) < j.N)) return false;
-    return split ? launch_fast_s<true>(j, st) : launch_fast_s<false>(j, st);
+    const bool rows = ci.es == 1 && co.es == 1;
+    const bool cols = !rows && labs(ci.vs) == 1 && labs(co.vs) == 1 && j.nvec >= 16;
+    if (rows) {
+        // rows of an in-place call must not overlap each other (each CTA reads its
+        // rows completely before it writes them)
+        if (j.nvec > 1 && (labs(ci.vs) < j.N || labs(co.vs) < j.N)) return false;
+        return split ? launch_fast_rows<true>(j, st) : launch_fast_rows<false>(j, st);
+    }
+    if (cols) {
+        // columns of an in-place call: each CTA reads all elements of its
+        // transforms before it writes them; transforms must not share elements
+        if (labs(ci.es) < j.nvec || labs(co.es) < j.nvec) return false;
+        return split ? launch_fast_cols<true>(j, st) : launch_fast_cols<false>(j, st);
+    }
+    return false;
 }
 
 }  // namespace jv
