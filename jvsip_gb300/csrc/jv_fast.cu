@@ -130,9 +130,11 @@ struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>, SPLIT, COLS> {
 // consecutive threads on adjacent transforms, so every load and store of a
 // warp covers RPC neighbouring elements of each row it touches; each
 // transform's shared-memory row has an odd pitch so the RPC rows fall in
-// different banks.
+// different banks.  The 512-thread column tiles are held to 64 registers so
+// two CTAs share an SM (with 86 registers one CTA's loads had no other CTA's
+// passes to overlap).
 template <int N, int T, int RPC, typename L, bool SPLIT, bool COLS>
-__global__ void __launch_bounds__(T *RPC) k_fast(const FastArgs pa) {
+__global__ void __launch_bounds__(T *RPC, (COLS && T * RPC == 512) ? 2 : 1) k_fast(const FastArgs pa) {
     constexpr int E = N / T;
     constexpr int R1 = L::first;
     constexpr int NP = N + N / 16 + (COLS ? 1 : 0);  // padded row in shared memory
