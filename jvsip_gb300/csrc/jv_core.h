@@ -119,6 +119,10 @@ struct Job {
     const void *tw_hi = nullptr;       //   group*tw_ys: tw_lo[m & tw_mask] * tw_hi[m >> tw_sh]
     unsigned tw_mask = 0, tw_sh = 0, tw_ts = 0, tw_ys = 0;
     struct LongPlan *lp = nullptr;     // the plan's long-transform decomposition (or null)
+    // a pass of a large-radix Stockham transform of 2^k points (radix N):
+    // Ns = product of the earlier radices (2^sp_lgns), input twiddle exponent
+    // stride Nt/(Ns*N), sp_mask = Nt - 1
+    unsigned sp_ns = 1, sp_lgns = 0, sp_twstride = 0, sp_mask = 0;
     // the k-omega pipeline (its own kernel instances): R2C rows tapered as they
     // are loaded -- real element n of transform t times taper_n[n*taper_n_st],
     // then times taper_t[t*taper_t_st], written back when taper_back -- and c2c
@@ -152,6 +156,10 @@ void count_launch_undo(unsigned long long n);  // launches recorded by a capture
 struct LongPlan {
     long N1 = 0, N2 = 0;
     struct Plan *p1 = nullptr, *p2 = nullptr;  // c2c plans of N1 and N2 points (schedules, tables)
+    // single vectors of 2^k points (f32): passes of radix sp_radix[i] (64..2048)
+    // in the register-resident kernel's column tiles, plans of those lengths
+    std::vector<long> sp_radix;
+    std::vector<struct Plan *> sp_plans;
     void *d_lo = nullptr, *d_hi = nullptr;     // two-level table of W_N^m: lo[m & mask] * hi[m >> sh]
     unsigned mask = 0, sh = 0;
     void *scratch = nullptr;                   // nvec * N complex, allocated at the first call
@@ -175,6 +183,9 @@ bool launch_global_f32(const Job &j, cudaStream_t s);
 bool launch_global_f64(const Job &j, cudaStream_t s);
 bool launch_fast_f32(const Job &j, cudaStream_t s);   // specialised kernels; false when none fits
 std::vector<int> fast_radices(long N);                // radix list of the specialised kernel for N
+bool fast_step_len(long N);                           // lengths the specialised kernel takes as long-transform steps
+bool launch_fast_step_f32(const Job &j, cudaStream_t s);  // a long-transform step in column-tile mode (single group)
+bool launch_fast_sp_f32(const Job &j, cudaStream_t s);    // a pass of a large-radix Stockham transform (sp_* set)
 bool launch_split_f32(const Job &j, cudaStream_t s);  // precision form; false when the call does not qualify
 bool launch_fast_dd(const Job &j, cudaStream_t s);    // FP64 form (double-float rows); false when it does not qualify
 std::vector<int> dd_radices(long N);                  // radix list of the FP64 form for N (empty: none)

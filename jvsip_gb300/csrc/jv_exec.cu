@@ -270,7 +270,7 @@ static bool step_job(Job &q, const Job &j, const Plan *sp) {
     q.tw = sp->d_tw;
     q.twg = sp->d_twg;
     q.pc = sp->d_pc;
-    q.twp = nullptr;
+    q.twp = sp->d_twp;
     q.thalf = nullptr;
     q.form = 0;
     q.no_fast = true;
@@ -302,11 +302,17 @@ static bool two_steps(const Job &j, LongPlan *lp, const CView &in, const CView &
     Job a = j, b = j;
     a.nvec = b.nvec = nv;
     if (!step_job(a, j, lp->p2) || !step_job(b, j, lp->p1)) return false;
-    // step A: transform over n2 (N2 points, element n1 + N1*n2 of x)
+    // step A: transform over n2 (N2 points, element n1 + N1*n2 of x).  With
+    // equal conjugations (c2c, R2C) each step conjugates on its own load and
+    // store -- an inverse transform of its own, the twiddle applied in the
+    // conjugated domain; otherwise (C2R: forward transform of conjugated data,
+    // conjugated at the end) step A conjugates the load and step B the store.
+    const bool same = conj_in == conj_out;
     a.cin = in;
     a.cout = scv;
     a.conj_in = conj_in;
-    a.conj_out = 0;
+    a.conj_out = same ? conj_in : 0;
+    if (same) a.inv = b.inv = conj_in;
     a.has_scale = 0;
     a.scale = 1.0;
     a.tw_lo = lp->d_lo;
@@ -316,7 +322,7 @@ static bool two_steps(const Job &j, LongPlan *lp, const CView &in, const CView &
     // step B: transform over n1 (N1 points) of the scratch, k1 to y[k2 + N2*k1]
     b.cin = scv;
     b.cout = out;
-    b.conj_in = 0;
+    b.conj_in = same ? conj_out : 0;
     b.conj_out = conj_out;
     b.has_scale = has_scale;
     b.scale = scale;
@@ -359,8 +365,72 @@ static bool two_steps(const Job &j, LongPlan *lp, const CView &in, const CView &
         b.cout.vs = out.vs;
         b.bvs_out = out.es;
     }
-    if (j.prec == P_F32) return launch_smem_f32(a, st) && launch_smem_f32(b, st);
+    if (j.prec == P_F32) {
+        // single groups of lengths the register-resident kernel takes as column tiles
+        const bool fa = a.nbatch == 1 && launch_fast_step_f32(a, st);
+        if (!fa && jvsip_gpu_last_error()) return false;
+        if (!fa && !launch_smem_f32(a, st)) return false;
+        const bool fb = b.nbatch == 1 && launch_fast_step_f32(b, st);
+        if (!fb && jvsip_gpu_last_error()) return false;
+        return fb || launch_smem_f32(b, st);
+    }
     return launch_smem_f64(a, st) && launch_smem_f64(b, st);
+}
+
+// A single vector of 2^n points (single precision, interleaved, unit stride)
+// as large-radix Stockham passes (LongPlan::sp_radix): pass p reads element n
+// of transform j at j + n*N/R_p, multiplies it by W_N^(n*m*N/(Ns*R_p)),
+// m = j mod Ns, and writes output k at (j - m)*R_p + m + k*Ns, Ns = R_0...R_{p-1};
+// the passes alternate between two scratch halves and the last one writes y.
+static bool sp_passes(const Job &j, LongPlan *lp, char *sc, size_t esz, cudaStream_t st) {
+    const long N = j.N;
+    const int k = (int)lp->sp_radix.size();
+    const size_t one = (size_t)N * 2 * esz;
+    unsigned long Ns = 1;
+    for (int p = 0; p < k; p++) {
+        const long R = lp->sp_radix[p];
+        Job q = j;
+        q.kind = K_C2C;
+        q.N = R;
+        q.nvec = N / R;
+        q.nbatch = 1;
+        q.lp = nullptr;
+        q.twp = lp->sp_plans[p]->d_twp;
+        q.twg = lp->sp_plans[p]->d_twg;
+        q.pc = lp->sp_plans[p]->d_pc;
+        q.npass = 0;
+        q.tw_lo = lp->d_lo;
+        q.tw_hi = lp->d_hi;
+        q.tw_mask = lp->mask;
+        q.tw_sh = lp->sh;
+        q.sp_ns = (unsigned)Ns;
+        unsigned lg = 0;
+        while ((1UL << lg) < Ns) lg++;
+        q.sp_lgns = lg;
+        q.sp_twstride = (unsigned)((unsigned long)N / (Ns * (unsigned long)R));
+        q.sp_mask = (unsigned)(N - 1);
+        q.has_scale = (p == k - 1) ? j.has_scale : 0;
+        CView in = j.cin, out = j.cout;
+        if (p > 0) {
+            char *b = sc + (size_t)((p - 1) % 2) * one;
+            in.re = b;
+            in.im = b + esz;
+            in.off = 0;
+        }
+        if (p < k - 1) {
+            char *b = sc + (size_t)(p % 2) * one;
+            out.re = b;
+            out.im = b + esz;
+            out.off = 0;
+        }
+        in.es = N / R;
+        in.vs = 1;
+        q.cin = in;
+        q.cout = out;
+        if (!launch_fast_sp_f32(q, st)) return false;
+        Ns *= (unsigned long)R;
+    }
+    return true;
 }
 
 // A real view of unit stride, even offset and pitch, 2-element aligned, as
@@ -394,7 +464,10 @@ static bool run_long(Job &j, cudaStream_t st, bool *handled) {
     if (j.kind == K_R2C && !(interleaved(j.cout, esz) && real_as_complex(j.rin, j.nvec, esz, &zin))) return false;
     const long N = j.N, nv = j.nvec;
     const size_t one = (size_t)nv * N * 2 * esz;
-    const size_t need = j.kind == K_C2R ? 2 * one : one;
+    // single c2c vectors of unit stride take the Stockham passes when planned
+    const bool sp = !lp->sp_radix.empty() && j.kind == K_C2C && nv == 1 && j.cin.es == 1 && j.cout.es == 1 &&
+                    j.prec == P_F32;
+    const size_t need = (j.kind == K_C2R || sp) ? 2 * one : one;
     *handled = true;
     if (lp->scratch_bytes < need) {
         // held by the plan (a captured call replays into it)
@@ -407,6 +480,7 @@ static bool run_long(Job &j, cudaStream_t st, bool *handled) {
         }
     }
     char *sc = (char *)lp->scratch;
+    if (sp) return sp_passes(j, lp, sc, esz, st);
     if (j.kind == K_C2C)
         return two_steps(j, lp, j.cin, j.cout, nv, j.inv, j.inv, j.has_scale, j.scale, sc, esz, st);
     if (j.kind == K_R2C) {
@@ -499,8 +573,10 @@ static bool run_job_planned(Plan *p, Job &j, cudaStream_t st) {
                                    (j.kind == K_R2C && interleaved(j.cout, esz) &&
                                     real_as_complex(j.rin, j.nvec, esz, &tmpv)) ||
                                    j.kind == K_C2R);
-    const bool long_ready =
-        long_job && j.lp->scratch_bytes >= (size_t)j.nvec * j.N * 2 * esz * (j.kind == K_C2R ? 2 : 1);
+    const bool sp_job = long_job && !j.lp->sp_radix.empty() && j.kind == K_C2C && j.nvec == 1 &&
+                        j.cin.es == 1 && j.cout.es == 1 && j.prec == P_F32;
+    const bool long_ready = long_job && j.lp->scratch_bytes >= (size_t)j.nvec * j.N * 2 * esz *
+                                                                 ((j.kind == K_C2R || sp_job) ? 2 : 1);
     if (!split && !job_in_smem(j) && !long_job) return run_job(j, st);
     CallGraph *e = nullptr;
     for (CallGraph &g : p->graphs)

@@ -37,6 +37,15 @@ struct FastArgs {
     // n of row v at [off + v*vs + n]
     const float *in_re, *in_im;
     float *out_re, *out_im;
+    // output twiddle of the first step of a long transform (TW instances):
+    // element k of transform g times W^(g*k) = tw_lo[m & tw_mask] * tw_hi[m >> tw_sh]
+    const float2 *tw_lo, *tw_hi;
+    unsigned tw_mask, tw_sh;
+    // one pass of a large-radix Stockham transform of Nt = 2^k points (SP
+    // instances; the kernel's N is the pass radix R): transform j reads
+    // element n at j + n*Nt/R (es_in), multiplies it by W_Nt^(n*m*Nt/(Ns*R))
+    // with m = j mod Ns, and writes output k at (j - m)*R + m + k*Ns
+    unsigned sp_ns, sp_lgns, sp_twstride, sp_mask;
     long off_in, vs_in, off_out, vs_out;
     long nvec;
     int inv;
@@ -85,10 +94,10 @@ __device__ __forceinline__ void store_pass(const float2 (&v)[E], float2 *s, int 
 }
 
 // Passes after the first.  On entry shared memory holds the previous pass's output.
-template <int N, int T, int E, int NsIn, int Off, typename L, bool SPLIT, bool COLS> struct Passes;
+template <int N, int T, int E, int NsIn, int Off, typename L, bool SPLIT, bool COLS, bool TW, bool SP> struct Passes;
 
-template <int N, int T, int E, int NsIn, int Off, int R0, int... Rs, bool SPLIT, bool COLS>
-struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>, SPLIT, COLS> {
+template <int N, int T, int E, int NsIn, int Off, int R0, int... Rs, bool SPLIT, bool COLS, bool TW, bool SP>
+struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>, SPLIT, COLS, TW, SP> {
     static __device__ __forceinline__ void run(float2 (&v)[E], float2 *s, int t, const FastArgs &a, long row,
                                                bool live) {
         __syncthreads();
@@ -97,7 +106,18 @@ struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>, SPLIT, COLS> {
         if constexpr (sizeof...(Rs) == 0) {
             // last pass: j < N/R0 = NsIn, so element j + r*NsIn -- coalesced stores
             if (live) {
-                const long ob = a.off_out + row * a.vs_out;
+                // base of the transform's outputs and the stride of output k:
+                // rows (1, 32-bit offsets), column tiles (es_out), Stockham
+                // passes ((row - m)*R + m + k*Ns)
+                long ob = a.off_out + row * a.vs_out;
+                long ks = COLS ? a.es_out : 1L;
+                if constexpr (SP) {
+                    const unsigned m = (unsigned)row & (a.sp_ns - 1u);
+                    ob = a.off_out + (long)((unsigned)row >> a.sp_lgns) * ((long)a.sp_ns * N) + m;
+                    ks = a.sp_ns;
+                }
+                float2 *o = a.out + ob;
+                float *orr = a.out_re + ob, *oi = a.out_im + ob;
                 constexpr int B = E / R0;
 #pragma unroll
                 for (int b = 0; b < B; b++) {
@@ -105,14 +125,27 @@ struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>, SPLIT, COLS> {
 #pragma unroll
                     for (int r = 0; r < R0; r++) {
                         float2 c = v[b * R0 + r];
+                        if constexpr (TW)
+                            c = cmul(c, tw_two_level(a.tw_lo, a.tw_hi, a.tw_mask, a.tw_sh,
+                                                     (unsigned)row * (unsigned)(j + r * NsIn)));
                         if (a.inv) c.y = -c.y;
                         if (a.has_scale) c = cscale(c, a.scale);
-                        const long e = ob + (long)(j + r * NsIn) * (COLS ? a.es_out : 1L);
-                        if constexpr (SPLIT) {
-                            a.out_re[e] = c.x;
-                            a.out_im[e] = c.y;
+                        const int k = j + r * NsIn;
+                        if constexpr (COLS) {
+                            const long e = (long)k * ks;
+                            if constexpr (SPLIT) {
+                                orr[e] = c.x;
+                                oi[e] = c.y;
+                            } else {
+                                o[e] = c;
+                            }
                         } else {
-                            a.out[e] = c;
+                            if constexpr (SPLIT) {
+                                orr[k] = c.x;
+                                oi[k] = c.y;
+                            } else {
+                                o[k] = c;
+                            }
                         }
                     }
                 }
@@ -120,7 +153,7 @@ struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>, SPLIT, COLS> {
         } else {
             __syncthreads();
             store_pass<N, T, E, R0>(v, s, t, NsIn);
-            Passes<N, T, E, NsIn * R0, Off + R0 * NsIn, RList<Rs...>, SPLIT, COLS>::run(v, s, t, a, row, live);
+            Passes<N, T, E, NsIn * R0, Off + R0 * NsIn, RList<Rs...>, SPLIT, COLS, TW, SP>::run(v, s, t, a, row, live);
         }
     }
 };
@@ -130,11 +163,14 @@ struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>, SPLIT, COLS> {
 // consecutive threads on adjacent transforms, so every load and store of a
 // warp covers RPC neighbouring elements of each row it touches; each
 // transform's shared-memory row has an odd pitch so the RPC rows fall in
-// different banks.  The 512-thread column tiles are held to 64 registers so
-// two CTAs share an SM (with 86 registers one CTA's loads had no other CTA's
-// passes to overlap).
-template <int N, int T, int RPC, typename L, bool SPLIT, bool COLS>
-__global__ void __launch_bounds__(T *RPC, (COLS && T * RPC == 512) ? 2 : 1) k_fast(const FastArgs pa) {
+// different banks.  CTAs of up to 512 threads are held to 64 registers so
+// that 1024 threads share an SM (ptxas otherwise took 86-115 registers, and one
+// or two CTAs per SM left a CTA's loads without other CTAs' passes to overlap);
+// the Stockham passes are not: measured on 2^24 points, their 256-point
+// passes took 69-85 us at 128 registers (23 % of warps active) and 98-119 us
+// at 64 (47 %).
+template <int N, int T, int RPC, typename L, bool SPLIT, bool COLS, bool TW, bool SP>
+__global__ void __launch_bounds__(T *RPC, (T * RPC <= 512 && !SP) ? 1024 / (T * RPC) : 1) k_fast(const FastArgs pa) {
     constexpr int E = N / T;
     constexpr int R1 = L::first;
     constexpr int NP = N + N / 16 + (COLS ? 1 : 0);  // padded row in shared memory
@@ -149,27 +185,67 @@ __global__ void __launch_bounds__(T *RPC, (COLS && T * RPC == 512) ? 2 : 1) k_fa
     const bool live = row < a.nvec;
     const long rowc = live ? row : a.nvec - 1;
     float2 v[E];
+    // base pointers of the transform; rows index them with 32-bit offsets
     const long ib = a.off_in + rowc * a.vs_in;
+    const float2 *inb = a.in + ib;
+    const float *inr = a.in_re + ib, *ini = a.in_im + ib;
     constexpr int B1 = E / R1;
 #pragma unroll
     for (int b = 0; b < B1; b++)
 #pragma unroll
         for (int r = 0; r < R1; r++) {
-            const long e = ib + (long)(t + T * b + r * (N / R1)) * (COLS ? a.es_in : 1L);
+            const int n = t + T * b + r * (N / R1);
             float2 c;
-            if constexpr (SPLIT) c = make_float2(a.in_re[e], a.in_im[e]);
-            else c = a.in[e];
+            if constexpr (COLS) {
+                const long e = (long)n * a.es_in;
+                if constexpr (SPLIT) c = make_float2(inr[e], ini[e]);
+                else c = inb[e];
+            } else {
+                if constexpr (SPLIT) c = make_float2(inr[n], ini[n]);
+                else c = inb[n];
+            }
             if (a.inv) c.y = -c.y;
+            if constexpr (SP) {
+                // Stockham input twiddle W_Nt^(n*m*stride), n = element index
+                const unsigned m = (unsigned)rowc & (a.sp_ns - 1u);
+                if (m) {
+                    const unsigned n = (unsigned)(t + T * b + r * (N / R1));
+                    c = cmul(c, tw_two_level(a.tw_lo, a.tw_hi, a.tw_mask, a.tw_sh,
+                                             (n * m * a.sp_twstride) & a.sp_mask));
+                }
+            }
             v[b * R1 + r] = c;
         }
     fast_bfly<N, T, R1, E, 1>(v, t, nullptr);
     store_pass<N, T, E, R1>(v, s, t, 1);
-    Passes<N, T, E, R1, R1, typename L::rest, SPLIT, COLS>::run(v, s, t, a, rowc, live);
+    if constexpr (SP) {
+        if (a.sp_ns == 1) {
+            // the first Stockham pass writes each transform's outputs
+            // contiguously (j*R + k): the passes after the first radix take
+            // the row mapping (T consecutive threads on one transform), so
+            // the last one's stores are coalesced
+            const int t2 = (int)threadIdx.x % T, rl2 = (int)threadIdx.x / T;
+            const long row2 = (long)blockIdx.x * RPC + rl2;
+            const bool live2 = row2 < a.nvec;
+            Passes<N, T, E, R1, R1, typename L::rest, SPLIT, COLS, TW, SP>::run(
+                v, reinterpret_cast<float2 *>(smem_raw) + rl2 * NP, t2, a, live2 ? row2 : a.nvec - 1, live2);
+            return;
+        }
+    }
+    Passes<N, T, E, R1, R1, typename L::rest, SPLIT, COLS, TW, SP>::run(v, s, t, a, rowc, live);
 }
 
-template <int N, int T, int RPC, typename L, bool SPLIT, bool COLS>
+template <int N, int T, int RPC, typename L, bool SPLIT, bool COLS, bool TW = false, bool SP = false>
 static bool launch_fast_n(const Job &j, cudaStream_t st) {
     FastArgs a;
+    a.sp_ns = j.sp_ns;
+    a.sp_lgns = j.sp_lgns;
+    a.sp_twstride = j.sp_twstride;
+    a.sp_mask = j.sp_mask;
+    a.tw_lo = (const float2 *)j.tw_lo;
+    a.tw_hi = (const float2 *)j.tw_hi;
+    a.tw_mask = j.tw_mask;
+    a.tw_sh = j.tw_sh;
     a.in = (const float2 *)j.cin.re;
     a.out = (float2 *)j.cout.re;
     a.es_in = j.cin.es;
@@ -193,14 +269,14 @@ static bool launch_fast_n(const Job &j, cudaStream_t st) {
     static bool attr = false;
     if (!attr) {
         if (smem > 48 * 1024 &&
-            !cuda_ok(cudaFuncSetAttribute(k_fast<N, T, RPC, L, SPLIT, COLS>,
+            !cuda_ok(cudaFuncSetAttribute(k_fast<N, T, RPC, L, SPLIT, COLS, TW, SP>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                      "cudaFuncSetAttribute"))
             return false;
         attr = true;
     }
     long grid = (j.nvec + RPC - 1) / RPC;
-    k_fast<N, T, RPC, L, SPLIT, COLS><<<(unsigned)grid, T * RPC, smem, st>>>(a);
+    k_fast<N, T, RPC, L, SPLIT, COLS, TW, SP><<<(unsigned)grid, T * RPC, smem, st>>>(a);
     count_launch();
     return cuda_ok(cudaGetLastError(), "k_fast launch");
 }
@@ -255,6 +331,54 @@ static bool launch_fast_cols(const Job &j, cudaStream_t st) {
         case 2048: return launch_fast_n<2048, 128, 4, RList<16, 16, 8>, SPLIT, true>(j, st);
         // 4096 points: two columns per CTA measured slower (1689 GB/s) than the
         // shared-memory kernel's four (1841 GB/s); it keeps those
+        default: return false;
+    }
+}
+
+// A step of a long transform (single vector: one group) in column-tile mode:
+// the first step with its output twiddle (TW) and row-contiguous output, the
+// second plain.  Both steps conjugate on load and store when inverse (each is
+// an inverse transform of its own; the first step's twiddle is applied in the
+// conjugated domain, which conjugates it).
+template <bool TW>
+static bool launch_fast_step_t(const Job &j, cudaStream_t st) {
+    switch (j.N) {
+        case 64: return launch_fast_n<64, 4, 64, RList<16, 4>, false, true, TW>(j, st);
+        case 128: return launch_fast_n<128, 8, 32, RList<16, 8>, false, true, TW>(j, st);
+        case 256: return launch_fast_n<256, 16, 16, RList<16, 16>, false, true, TW>(j, st);
+        case 512: return launch_fast_n<512, 32, 16, RList<16, 16, 2>, false, true, TW>(j, st);
+        case 1000: return launch_fast_n<1000, 100, 8, RList<10, 10, 10>, false, true, TW>(j, st);
+        case 1024: return launch_fast_n<1024, 64, 8, RList<16, 16, 4>, false, true, TW>(j, st);
+        case 2048: return launch_fast_n<2048, 128, 4, RList<16, 16, 8>, false, true, TW>(j, st);
+        case 4096: return launch_fast_n<4096, 256, 2, RList<16, 16, 16>, false, true, TW>(j, st);
+        default: return false;
+    }
+}
+
+bool fast_step_len(long N) {
+    return N == 64 || N == 128 || N == 256 || N == 512 || N == 1000 || N == 1024 || N == 2048 || N == 4096;
+}
+
+bool launch_fast_step_f32(const Job &j, cudaStream_t st) {
+    if (j.kind != K_C2C || j.prec != P_F32 || j.nbatch != 1 || !fast_step_len(j.N) || !j.twp) return false;
+    const int ci = j.conj_in < 0 ? j.inv : j.conj_in, co = j.conj_out < 0 ? j.inv : j.conj_out;
+    if (ci != j.inv || co != j.inv) return false;
+    const CView &a = j.cin, &b = j.cout;
+    if (a.cst != 2 || b.cst != 2 || (const float *)a.im != (const float *)a.re + 1 ||
+        (const float *)b.im != (const float *)b.re + 1 || ((uintptr_t)a.re % 8) || ((uintptr_t)b.re % 8))
+        return false;
+    return j.tw_lo ? launch_fast_step_t<true>(j, st) : launch_fast_step_t<false>(j, st);
+}
+
+// One pass of a large-radix Stockham transform (j.sp_* set; radix j.N).
+bool launch_fast_sp_f32(const Job &j, cudaStream_t st) {
+    switch (j.N) {
+        case 64: return launch_fast_n<64, 4, 64, RList<16, 4>, false, true, false, true>(j, st);
+        case 128: return launch_fast_n<128, 8, 32, RList<16, 8>, false, true, false, true>(j, st);
+        case 256: return launch_fast_n<256, 16, 16, RList<16, 16>, false, true, false, true>(j, st);
+        case 512: return launch_fast_n<512, 32, 16, RList<16, 16, 2>, false, true, false, true>(j, st);
+        case 1024: return launch_fast_n<1024, 64, 8, RList<16, 16, 4>, false, true, false, true>(j, st);
+        case 2048: return launch_fast_n<2048, 128, 4, RList<16, 16, 8>, false, true, false, true>(j, st);
         default: return false;
     }
 }

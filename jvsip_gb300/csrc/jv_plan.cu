@@ -327,6 +327,11 @@ static void long_free(LongPlan *lp) {
             release_tables(q);
             delete q;
         }
+    for (Plan *q : lp->sp_plans)
+        if (q) {
+            release_tables(q);
+            delete q;
+        }
     dfree(lp->d_lo);
     dfree(lp->d_hi);
     dfree(lp->scratch);
@@ -419,6 +424,37 @@ static bool build_long(Plan *p) {
         !cuda_ok(cudaMemcpy(lp->d_hi, hi.data(), hi.size() * sizeof(T), cudaMemcpyHostToDevice), "twiddle upload")) {
         long_free(lp);
         return false;
+    }
+    // single vectors of 2^n points, n >= 13 (single precision): large-radix
+    // Stockham passes of 2^6..2^11 points each, larger first -- two up to
+    // 2^22 points (fewer launches for short vectors), else ceil(n/9)
+    if (p->prec == P_F32 && (N & (N - 1)) == 0 && bits >= 13 && bits <= 31) {
+        const unsigned k = bits <= 22 ? 2 : (bits + 8) / 9;
+        std::vector<long> rad;
+        for (unsigned i = 0; i < k; i++) rad.push_back(1L << (bits / k + (i < bits % k ? 1 : 0)));
+        bool ok = true;
+        for (long R : rad) ok = ok && R >= 64 && R <= 2048;
+        for (size_t i = 0; ok && i < rad.size(); i++) {
+            Plan *q = step_plan<T>(rad[i], p->prec);
+            if (!q || !q->d_twp) {
+                if (q) {
+                    release_tables(q);
+                    delete q;
+                }
+                ok = false;
+                break;
+            }
+            lp->sp_plans.push_back(q);
+        }
+        if (ok) lp->sp_radix = rad;
+        else {
+            for (Plan *q : lp->sp_plans) {
+                release_tables(q);
+                delete q;
+            }
+            lp->sp_plans.clear();
+            jvsip_gpu_clear_error();
+        }
     }
     p->lp = lp;
     return true;
