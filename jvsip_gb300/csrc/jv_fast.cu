@@ -379,6 +379,7 @@ bool launch_fast_sp_f32(const Job &j, cudaStream_t st) {
         case 512: return launch_fast_n<512, 32, 16, RList<16, 16, 2>, false, true, false, true>(j, st);
         case 1024: return launch_fast_n<1024, 64, 8, RList<16, 16, 4>, false, true, false, true>(j, st);
         case 2048: return launch_fast_n<2048, 128, 4, RList<16, 16, 8>, false, true, false, true>(j, st);
+        case 4096: return launch_fast_n<4096, 256, 2, RList<16, 16, 16>, false, true, false, true>(j, st);
         default: return false;
     }
 }

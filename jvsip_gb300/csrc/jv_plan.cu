@@ -426,14 +426,14 @@ static bool build_long(Plan *p) {
         return false;
     }
     // single vectors of 2^n points, n >= 13 (single precision): large-radix
-    // Stockham passes of 2^6..2^11 points each, larger first -- two up to
-    // 2^22 points (fewer launches for short vectors), else ceil(n/9)
+    // Stockham passes of 2^6..2^12 points each, larger first -- two up to
+    // 2^23 points (fewer launches for short vectors), else ceil(n/9)
     if (p->prec == P_F32 && (N & (N - 1)) == 0 && bits >= 13 && bits <= 31) {
-        const unsigned k = bits <= 22 ? 2 : (bits + 8) / 9;
+        const unsigned k = bits <= 23 ? 2 : (bits + 8) / 9;
         std::vector<long> rad;
         for (unsigned i = 0; i < k; i++) rad.push_back(1L << (bits / k + (i < bits % k ? 1 : 0)));
         bool ok = true;
-        for (long R : rad) ok = ok && R >= 64 && R <= 2048;
+        for (long R : rad) ok = ok && R >= 64 && R <= 4096;
         for (size_t i = 0; ok && i < rad.size(); i++) {
             Plan *q = step_plan<T>(rad[i], p->prec);
             if (!q || !q->d_twp) {
