@@ -38,7 +38,7 @@ def rnd(n, seed):
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f", "d"])
-@pytest.mark.parametrize("N", [16807 * 2, 32768, 40000, 65536, 3 ** 10, 2 ** 17, 5 ** 7, 7 ** 6, 1 << 20])
+@pytest.mark.parametrize("N", [16807 * 2, 32768, 40000, 65536, 3 ** 10, 2 ** 17, 5 ** 7, 7 ** 6, 1 << 20, 1 << 23])
 def test_long_single_fft(N, dtype):
     z = rnd(N, N)
     x = interleave(z, dtype)
@@ -210,6 +210,32 @@ def test_long_real_vector_strided(stride):
     J.FFT(J.KIND_CROP, N, 1.0 / N).crfftop(vz, vb)
     assert rel(cplx(z), np.fft.rfft(xr)) <= tol(N // 2, np.float32)
     assert rel(back[off + stride * np.arange(N)].astype(np.float64), xr) <= 2 * tol(N // 2, np.float32)
+    for v in (vx, vz, vb):
+        v.destroy()
+    for b in (bx, bz, bb):
+        b.destroy()
+
+
+@pytest.mark.parametrize("N", [1 << 25])
+def test_long_real_vector_stockham_passes(N):
+    """Real vectors whose half length takes three Stockham passes (2^24
+    complex points): R2C through the passes and the in-place split, C2R back
+    through the two steps, against numpy's rfft."""
+    g = np.random.default_rng(17)
+    x = g.standard_normal(N, dtype=np.float32)
+    z = np.zeros(2 * (N // 2 + 1), np.float32)
+    back = np.zeros_like(x)
+    bx, bz, bb = J.RBlock(x), J.CBlock(z), J.RBlock(back)
+    for b in (bx, bz, bb):
+        b.admit(True)
+    vx, vz, vb = bx.vview(0, 1, N), bz.vview(0, 1, N // 2 + 1), bb.vview(0, 1, N)
+    J.FFT(J.KIND_RCOP, N, 0.5).rcfftop(vx, vz)
+    J.FFT(J.KIND_CROP, N, 2.0 / N).crfftop(vz, vb)
+    bz.sync()
+    bb.sync()
+    ref = 0.5 * np.fft.rfft(x.astype(np.float64))
+    assert rel(cplx(z), ref) <= tol(N // 2, np.float32)
+    assert rel(back.astype(np.float64), x.astype(np.float64)) <= 2 * tol(N // 2, np.float32)
     for v in (vx, vz, vb):
         v.destroy()
     for b in (bx, bz, bb):
