@@ -473,7 +473,10 @@ static bool run_long(Job &j, cudaStream_t st, bool *handled) {
     // in the two steps, 815 in two passes; 2^26 points 715 against 891)
     const bool sp = !lp->sp_radix.empty() && nv == 1 && j.prec == P_F32 && j.cout.es == 1 &&
                     ((j.kind == K_C2C && j.cin.es == 1) || (j.kind == K_R2C && lp->sp_radix.size() >= 3));
-    const size_t need = (j.kind == K_C2R || sp) ? 2 * one : one;
+    // the scratch is sized once for every path of the plan (twice the data:
+    // the passes and C2R use two halves): a captured call's graph holds its
+    // address, so it is never reallocated while the plan lives
+    const size_t need = 2 * one;
     *handled = true;
     if (lp->scratch_bytes < need) {
         // held by the plan (a captured call replays into it)
@@ -581,11 +584,7 @@ static bool run_job_planned(Plan *p, Job &j, cudaStream_t st) {
                                    (j.kind == K_R2C && interleaved(j.cout, esz) &&
                                     real_as_complex(j.rin, j.nvec, esz, &tmpv)) ||
                                    j.kind == K_C2R);
-    const bool sp_job = long_job && !j.lp->sp_radix.empty() && j.nvec == 1 && j.prec == P_F32 &&
-                        j.cout.es == 1 &&
-                        ((j.kind == K_C2C && j.cin.es == 1) || (j.kind == K_R2C && j.lp->sp_radix.size() >= 3));
-    const bool long_ready = long_job && j.lp->scratch_bytes >= (size_t)j.nvec * j.N * 2 * esz *
-                                                                 ((j.kind == K_C2R || sp_job) ? 2 : 1);
+    const bool long_ready = long_job && j.lp->scratch_bytes >= (size_t)j.nvec * j.N * 2 * esz * 2;
     if (!split && !job_in_smem(j) && !long_job) return run_job(j, st);
     CallGraph *e = nullptr;
     for (CallGraph &g : p->graphs)

@@ -240,3 +240,38 @@ def test_long_real_vector_stockham_passes(N):
         v.destroy()
     for b in (bx, bz, bb):
         b.destroy()
+
+
+def test_long_plan_scratch_stays_put_across_paths():
+    """A plan created with ntimes == 0 captures its strided calls (two steps)
+    and its unit-stride calls (Stockham passes) as graphs over one scratch; the
+    strided call's graph replayed after the unit-stride calls is still right."""
+    N = 65536
+    z = rnd(N, 23)
+    x2 = interleave(np.repeat(z, 2), np.float32)        # element n at 2n (stride 2)
+    x1 = interleave(z, np.float32)
+    y2, y1 = np.zeros(2 * N, np.float32), np.zeros(2 * N, np.float32)
+    b2, b1, c2, c1 = J.CBlock(x2), J.CBlock(x1), J.CBlock(y2), J.CBlock(y1)
+    for b in (b2, b1, c2, c1):
+        b.admit(True)
+    p = J.FFT(J.KIND_CCOP, N, 1.0, J.VSIP_FFT_FWD, ntimes=0)
+    v2, v1, w2, w1 = b2.vview(0, 2, N), b1.vview(0, 1, N), c2.vview(0, 1, N), c1.vview(0, 1, N)
+    ref = np.fft.fft(z)
+    for _ in range(3):
+        p.ccfftop(v2, w2)
+    for _ in range(3):
+        p.ccfftop(v1, w1)
+    c2.sync()
+    y2[:] = 0
+    c2.release(False)
+    c2.admit(True)
+    p.ccfftop(v2, w2)
+    c1.sync()
+    c2.sync()
+    assert int(J.lib().jvsip_fftm_graphs(p.h)) == 2
+    assert rel(cplx(y1), ref) <= tol(N, np.float32)
+    assert rel(cplx(y2), ref) <= tol(N, np.float32)
+    for v in (v2, v1, w2, w1):
+        v.destroy()
+    for b in (b2, b1, c2, c1):
+        b.destroy()
