@@ -182,6 +182,7 @@ bool launch_smem_real_f64(const Job &j, cudaStream_t s);
 bool launch_global_f32(const Job &j, cudaStream_t s);
 bool launch_global_f64(const Job &j, cudaStream_t s);
 bool launch_fast_f32(const Job &j, cudaStream_t s);   // specialised kernels; false when none fits
+bool launch_fast_real_f32(const Job &j, cudaStream_t s);  // R2C / C2R rows on the specialised kernel
 std::vector<int> fast_radices(long N);                // radix list of the specialised kernel for N
 bool fast_step_len(long N);                           // lengths the specialised kernel takes as long-transform steps
 bool launch_fast_step_f32(const Job &j, cudaStream_t s);  // a long-transform step in column-tile mode (single group)
