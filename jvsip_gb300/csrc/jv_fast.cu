@@ -9,8 +9,9 @@
 // global memory directly (element t + T*b + r*N/Rp, again coalesced): the
 // self-sorting Stockham order needs no digit-reversal pass, so every point is
 // read from and written to HBM exactly once.  Shared memory is indexed
-// i + (i >> 4), which makes every pass's stores and loads conflict-free for
-// 8-byte elements.  Several transforms share a CTA when N is small.
+// i + (i >> 4) (power-of-two passes conflict-free for 8-byte elements) with
+// row pitches chosen per tile shape (fast_pitch).  Several transforms share a
+// CTA when N is small.
 #include <stdio.h>
 #include <stdlib.h>
 

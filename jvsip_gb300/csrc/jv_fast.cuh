@@ -9,8 +9,9 @@
 // global memory directly (element t + T*b + r*N/Rp, again coalesced): the
 // self-sorting Stockham order needs no digit-reversal pass, so every point is
 // read from and written to HBM exactly once.  Shared memory is indexed
-// i + (i >> 4), which makes every pass's stores and loads conflict-free for
-// 8-byte elements.  Several transforms share a CTA when N is small.
+// i + (i >> 4) (power-of-two passes conflict-free for 8-byte elements) with
+// row pitches chosen per tile shape (fast_pitch).  Several transforms share a
+// CTA when N is small.
 //
 // Real rows (RM = 1: R2C, RM = 2: C2R) hold the half-length complex
 // transform: the R2C first pass reads x_{2n}, x_{2n+1} as one complex element
@@ -36,7 +37,25 @@ template <int R0, int... Rs> struct RList<R0, Rs...> {
 };
 template <> struct RList<> {};
 
-__device__ __forceinline__ int padx(int i) { return i + (i >> 4); }
+// Shared-memory index padding: one element per 16, or per 32 for the
+// 1000-point (10 x 10 x 10) and 768-point (12 x 8 x 8) transforms, whose
+// radix-10 and radix-12 strides collide less that way (2.6 and 1.75 wavefronts
+// per 64-bit access on average become 1.7 and 1.5).
+template <int N> constexpr int fast_pad_shift() { return (N == 1000 || N == 768) ? 5 : 4; }
+template <int N> __device__ __forceinline__ int padx(int i) { return i + (i >> fast_pad_shift<N>()); }
+
+// Padded pitch of a transform's row in shared memory.  Column tiles put
+// 16/RPC transforms' elements t, t+1, ... and RPC columns in one half-warp's
+// 64-bit access, so the RPC rows start 16/RPC elements apart modulo 16 (RPC <=
+// 8) or one element apart: every access then hits 32 distinct banks (an odd
+// pitch alone gave 2 wavefronts per access for 1024-point tiles of 8 columns
+// and 4 for 2048-point tiles of 4).
+template <int N, int RPC, bool COLS> constexpr int fast_pitch() {
+    constexpr int base = N + (N >> fast_pad_shift<N>());
+    if (!COLS) return base;
+    if (RPC > 8) return base + 1;
+    return base + (16 / RPC - base % 16 + 16) % 16;
+}
 
 struct FastArgs {
     const float2 *in;   // transform v starts at in + off_in + v*vs_in, element n at + n*es_in
@@ -87,7 +106,7 @@ __device__ __forceinline__ void load_pass(float2 (&v)[E], const float2 *s, int t
 #pragma unroll
     for (int b = 0; b < B; b++)
 #pragma unroll
-        for (int r = 0; r < R; r++) v[b * R + r] = s[padx(t + T * b + r * (N / R))];
+        for (int r = 0; r < R; r++) v[b * R + r] = s[padx<N>(t + T * b + r * (N / R))];
 }
 
 template <int N, int T, int E, int R>
@@ -99,7 +118,7 @@ __device__ __forceinline__ void store_pass(const float2 (&v)[E], float2 *s, int 
         int m = j % Ns;
         int base = (j - m) * R + m;
 #pragma unroll
-        for (int r = 0; r < R; r++) s[padx(base + r * Ns)] = v[b * R + r];
+        for (int r = 0; r < R; r++) s[padx<N>(base + r * Ns)] = v[b * R + r];
     }
 }
 
@@ -117,13 +136,13 @@ __device__ __forceinline__ void r2c_finish(const float2 (&v)[E], float2 *s, int 
     for (int b = 0; b < B; b++) {
         const int j = t + T * b;
 #pragma unroll
-        for (int r = 0; r < R; r++) s[padx(j + r * Ns)] = v[b * R + r];
+        for (int r = 0; r < R; r++) s[padx<N>(j + r * Ns)] = v[b * R + r];
     }
     __syncthreads();
     if (!live) return;
     float2 *o = a.out + a.off_out + row * a.vs_out;
     auto split = [&](int k) {
-        float2 f = s[padx(k == N ? 0 : k)], b = s[padx(k == 0 ? 0 : N - k)];
+        float2 f = s[padx<N>(k == N ? 0 : k)], b = s[padx<N>(k == 0 ? 0 : N - k)];
         if (a.has_scale) {
             f = cscale(f, a.scale);
             b = cscale(b, a.scale);
@@ -228,7 +247,7 @@ template <int N, int T, int RPC, typename L, bool SPLIT, bool COLS, bool TW, boo
 __global__ void __launch_bounds__(T *RPC, fast_min_blocks<N, T, RPC, SP>()) k_fast(const FastArgs pa) {
     constexpr int E = N / T;
     constexpr int R1 = L::first;
-    constexpr int NP = N + N / 16 + (COLS ? 1 : 0);  // padded row in shared memory
+    constexpr int NP = fast_pitch<N, RPC, COLS>();  // padded row in shared memory
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const FastArgs a = pa;
     const int t = COLS ? (int)threadIdx.x / RPC : (int)threadIdx.x % T;
@@ -343,7 +362,7 @@ static bool launch_fast_n(const Job &j, cudaStream_t st) {
         a.inv = 1;
     }
     if (!a.twp || (RM != 0 && !a.thalf)) return false;
-    constexpr int NP = N + N / 16 + (COLS ? 1 : 0);
+    constexpr int NP = fast_pitch<N, RPC, COLS>();
     size_t smem = (size_t)RPC * NP * sizeof(float2);
     static bool attr = false;
     if (!attr) {

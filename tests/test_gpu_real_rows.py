@@ -1,6 +1,6 @@
 """R2C and C2R rows on the register-resident kernel (vsip_rcfftmop_f /
 vsip_crfftmop_f with real rows of unit stride, even offset and even pitch):
-every half length it holds (64 .. 8192, 768 = 12*8*8, 1000 = 10*10*10), row
+every half length it holds (64 .. 8192, 768 = 8*8*12, 1000 = 10*10*10), row
 counts that leave the last CTA partly empty, pitched and offset rows, a scale
 on the forward transform, against numpy's FP64 rfft / irfft at the acceptance
 tolerance (rel-L2 <= 1e-6 log2 N); the same calls on the shared-memory kernel
