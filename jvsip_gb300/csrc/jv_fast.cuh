@@ -125,8 +125,9 @@ __device__ __forceinline__ void store_pass(const float2 (&v)[E], float2 *s, int 
 // R2C rows: the last pass's Z_k (k = j + r*Ns) to shared memory in natural
 // order, then X_k = ((Z_k + conj Z_{N-k}) - i w_k (Z_k - conj Z_{N-k}))/2 for
 // k = 0..N (Z_N = Z_0; w_k = exp(-i pi k/N)), the scale applied to Z first as
-// the reference does (VI_rcfftmop_f_def.h:79-118); thread t writes
-// X_{t + T*i} (coalesced) and thread 0 also X_N.
+// the reference does (VI_rcfftmop_f_def.h:79-118).  The thread of pair
+// (k, N-k), k = t + T*i <= N/2, reads Z_k and Z_{N-k} once and writes X_k and
+// X_{N-k} (X_N for k = 0): ascending and descending coalesced stores.
 template <int N, int T, int E, int R>
 __device__ __forceinline__ void r2c_finish(const float2 (&v)[E], float2 *s, int t, const FastArgs &a, long row,
                                            bool live, int Ns) {
@@ -141,19 +142,24 @@ __device__ __forceinline__ void r2c_finish(const float2 (&v)[E], float2 *s, int 
     __syncthreads();
     if (!live) return;
     float2 *o = a.out + a.off_out + row * a.vs_out;
-    auto split = [&](int k) {
-        float2 f = s[padx<N>(k == N ? 0 : k)], b = s[padx<N>(k == 0 ? 0 : N - k)];
-        if (a.has_scale) {
-            f = cscale(f, a.scale);
-            b = cscale(b, a.scale);
-        }
-        const float2 w = __ldg(&a.thalf[k]);
-        o[k] = make_float2(0.5f * (b.x + f.x + w.x * (b.y + f.y) + w.y * (f.x - b.x)),
-                           0.5f * (f.y - b.y + w.x * (b.x - f.x) + w.y * (b.y + f.y)));
-    };
+    constexpr int NPAIR = N / 2 + 1;
 #pragma unroll
-    for (int i = 0; i < E; i++) split(t + T * i);
-    if (t == 0) split(N);
+    for (int i = 0; i < (NPAIR + T - 1) / T; i++) {
+        const int k = t + T * i;
+        if (k >= NPAIR) break;
+        const int nk = (k == 0) ? N : N - k;
+        float2 zk = s[padx<N>(k)], zn = s[padx<N>(k == 0 ? 0 : N - k)];
+        if (a.has_scale) {
+            zk = cscale(zk, a.scale);
+            zn = cscale(zn, a.scale);
+        }
+        const float2 w = __ldg(&a.thalf[k]), w2 = __ldg(&a.thalf[nk]);
+        o[k] = make_float2(0.5f * (zn.x + zk.x + w.x * (zn.y + zk.y) + w.y * (zk.x - zn.x)),
+                           0.5f * (zk.y - zn.y + w.x * (zn.x - zk.x) + w.y * (zn.y + zk.y)));
+        if (nk != k)
+            o[nk] = make_float2(0.5f * (zk.x + zn.x + w2.x * (zk.y + zn.y) + w2.y * (zn.x - zk.x)),
+                                0.5f * (zn.y - zk.y + w2.x * (zk.x - zn.x) + w2.y * (zk.y + zn.y)));
+    }
 }
 
 // Passes after the first.  On entry shared memory holds the previous pass's output.
