@@ -130,6 +130,148 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
     for (int i = 0; i < 16; i++) v[16 + i] = t[i];
 }
 
+// ---- the steps of one group of 4 rows, shared by both kernels
+
+// step 1 operand from the thread's vector b = l of row w (v[a] = x[32a + l],
+// scaled by s1): A1[(w, b)][part*64 + ri*32 + a], K-blocks ab (re hi), 4+ab
+// (im hi), 8+ab (re lo), 12+ab (im lo)
+template <bool BF>
+__device__ __forceinline__ void sp_operand1(unsigned char *Asm, int w, int l, const float2 (&v)[32], float s1) {
+    unsigned char *arow = Asm + core_off(w * 32 + l, 0, SP_A_LBO);
+#pragma unroll
+    for (int ab = 0; ab < 4; ab++) {
+        uint4 hr, hi, lr, li;
+        uint32_t *phr = &hr.x, *phi = &hi.x, *plr = &lr.x, *pli = &li.x;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const float2 e0 = v[ab * 8 + 2 * q], e1 = v[ab * 8 + 2 * q + 1];
+            split2<BF>(e0.x * s1, e1.x * s1, phr[q], plr[q]);
+            split2<BF>(e0.y * s1, e1.y * s1, phi[q], pli[q]);
+        }
+        *reinterpret_cast<uint4 *>(arow + (0 + ab) * SP_A_LBO) = hr;
+        *reinterpret_cast<uint4 *>(arow + (4 + ab) * SP_A_LBO) = hi;
+        *reinterpret_cast<uint4 *>(arow + (8 + ab) * SP_A_LBO) = lr;
+        *reinterpret_cast<uint4 *>(arow + (12 + ab) * SP_A_LBO) = li;
+    }
+}
+
+// step 1 result (lane (w, l) = (row, b), columns re c | im c) times the
+// twiddle w1024^(b c), then the step 2 operand A2[(w, c)][part*64 + ri*32 + b]
+// written over step 1's; returns the step's power-of-two scale.  Lane pairs
+// (l, l^1) trade one word so that each lane stores two 4-byte pairs of
+// adjacent b: even lanes (re hi, im hi) at b = l, odd lanes (re lo, im lo) at
+// b = l - 1; the two stores are ordered so the even and odd halves of the
+// warp fall in different banks.
+template <bool BF>
+__device__ __forceinline__ float sp_operand2(unsigned char *Asm, int w, int l, float (&zr)[32], float (&zi)[32],
+                                             const float2 *__restrict__ tw) {
+    float mx = 0.f;
+#pragma unroll
+    for (int c = 0; c < 32; c++) {
+        const float2 t = __ldg(&tw[c * 32 + l]);
+        const float r = zr[c] * t.x - zi[c] * t.y, i = zr[c] * t.y + zi[c] * t.x;
+        zr[c] = r;
+        zi[c] = i;
+        mx = fmaxf(mx, fmaxf(fabsf(r), fabsf(i)));
+    }
+    const float s2 = BF ? 1.f : warp_scale(mx);
+    const bool even = (l & 1) == 0;
+    const int k1 = even ? l : 96 + l - 1, k2 = even ? 32 + l : 64 + l - 1;
+    unsigned char *p1 = Asm + core_off(w * 32, k1, SP_A_LBO);
+    unsigned char *p2 = Asm + core_off(w * 32, k2, SP_A_LBO);
+#pragma unroll
+    for (int c = 0; c < 32; c++) {
+        uint32_t P, Q;  // (re hi | im hi << 16), (re lo | im lo << 16)
+        split2<BF>(zr[c] * s2, zi[c] * s2, P, Q);
+        const uint32_t R = __shfl_xor_sync(0xffffffffu, even ? Q : P, 1);
+        const uint32_t X = even ? P : R, Y = even ? R : Q;
+        const uint32_t wlo = __byte_perm(X, Y, 0x5410), whi = __byte_perm(X, Y, 0x7632);
+        const uint32_t mo = (uint32_t)((c >> 3) << 7) + (uint32_t)((c & 7) << 4);
+        *reinterpret_cast<uint32_t *>(p1 + mo) = even ? wlo : whi;
+        *reinterpret_cast<uint32_t *>(p2 + mo) = even ? whi : wlo;
+    }
+    return s2;
+}
+
+// step 2 result: lane (w, l) = (row, c = l), columns re d | im d -> out[c + 32 d]
+__device__ __forceinline__ void sp_store(const SplitArgs &a, uint32_t lane_base, long row, int l, float f) {
+    float yr[32], yi[32];
+    tmem_ld32(lane_base + 0, yr);
+    tmem_ld32(lane_base + 32, yi);
+    tc::tmem_ld_wait();
+    if (row < a.nvec) {
+        float2 *dst = a.out + a.off_out + row * a.vs_out;
+#pragma unroll
+        for (int d = 0; d < 32; d++) {
+            float2 o = make_float2(yr[d] * f, yi[d] * f);
+            if (a.inv) o.y = -o.y;
+            dst[l + 32 * d] = o;
+        }
+    }
+}
+
+// B operand (constant per plan) into shared memory
+__device__ __forceinline__ void sp_load_b(unsigned char *Bsm, const uint4 *__restrict__ bop, int tid) {
+    uint4 *dst = reinterpret_cast<uint4 *>(Bsm);
+#pragma unroll
+    for (int i = 0; i < SP_B_BYTES / 16 / 128; i++) dst[tid + 128 * i] = __ldg(&bop[tid + 128 * i]);
+}
+
+// Steps 1 and 2 of the group whose rows the threads hold in v (conjugated when
+// inverse): operand, MMAs, twiddle, operand, MMAs, store.  Returns false when
+// a barrier wait expired (uniform over the CTA); *pending is then the MMA
+// barrier phase still outstanding (2: none).
+template <bool BF>
+__device__ __forceinline__ bool sp_group(const SplitArgs &a, unsigned char *Asm, uint32_t a0, uint32_t b0,
+                                         uint32_t tbase, uint64_t *mbar, float2 (&v)[32], long row, int tid,
+                                         uint32_t *pending) {
+    const int w = tid >> 5, l = tid & 31;
+    float mx = 0.f;
+#pragma unroll
+    for (int i = 0; i < 32; i++) mx = fmaxf(mx, fmaxf(fabsf(v[i].x), fabsf(v[i].y)));
+    const float s1 = BF ? 1.f : warp_scale(mx);
+    sp_operand1<BF>(Asm, w, l, v, s1);
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t idesc = tc::idesc_f16(SPM, SPNN, BF ? 1 : 0);
+    if (tid == 0) {
+        split_mma(tbase, a0, b0, idesc);
+        tc::mma_commit(mbar);
+    }
+    bool ok = tc::mbar_wait(mbar, 0, SP_WAIT_LIMIT);
+    ok = __syncthreads_and(ok);
+    *pending = ok ? 2u : 0u;
+    tc::fence_after_sync();
+    if (!ok) return false;
+    const uint32_t lane_base = tbase + ((uint32_t)(w * 32) << 16);
+    float zr[32], zi[32];
+    tmem_ld32(lane_base + 0, zr);
+    tmem_ld32(lane_base + 32, zi);
+    tc::tmem_ld_wait();
+    const float s2 = sp_operand2<BF>(Asm, w, l, zr, zi, a.tw);
+    // the step 1 accumulator is read out: step 2 reuses its columns
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (tid == 0) {
+        split_mma(tbase, a0, b0, idesc);
+        tc::mma_commit(mbar);
+    }
+    ok = tc::mbar_wait(mbar, 1, SP_WAIT_LIMIT);
+    ok = __syncthreads_and(ok);
+    *pending = ok ? 2u : 1u;
+    tc::fence_after_sync();
+    if (!ok) return false;
+    sp_store(a, lane_base, row, l, (a.has_scale ? a.scale : 1.f) / (s1 * s2));
+    // the accumulator is read out before the next group's step 1 writes it
+    tc::fence_before_sync();
+    return true;
+}
+
+// One group per CTA (any 8-byte aligned rows).
 template <bool BF>
 __global__ void __launch_bounds__(128, 4) k_split1024(const SplitArgs a) {
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -140,144 +282,34 @@ __global__ void __launch_bounds__(128, 4) k_split1024(const SplitArgs a) {
     const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
     const long row = (long)blockIdx.x * 4 + w;
     const bool live = row < a.nvec;
-
     if (w == 0) {
         tc::tmem_alloc(&tslot, SP_TMEM_COLS);
         tc::tmem_relinquish();
     }
     if (tid == 0) tc::mbar_init(&mbar, 1);
-    // B operand (constant per plan) into shared memory
-    {
-        uint4 *dst = reinterpret_cast<uint4 *>(Bsm);
-#pragma unroll
-        for (int i = 0; i < SP_B_BYTES / 16 / 128; i++) dst[tid + 128 * i] = __ldg(&a.bop[tid + 128 * i]);
-    }
-    // ---- step 1 operand: thread (w, l) owns vector b = l of row w: x[32a + l], a < 32
+    sp_load_b(Bsm, a.bop, tid);
+    // thread (w, l) owns vector b = l of row w: x[32a + l], a < 32
     float2 v[32];
     const float2 *src = a.in + a.off_in + (live ? row : 0) * a.vs_in;
-    float mx = 0.f;
 #pragma unroll
     for (int i = 0; i < 32; i++) {
         float2 c = live ? src[32 * i + l] : make_float2(0.f, 0.f);
         if (a.inv) c.y = -c.y;
         v[i] = c;
-        mx = fmaxf(mx, fmaxf(fabsf(c.x), fabsf(c.y)));
     }
-    const float s1 = BF ? 1.f : warp_scale(mx);
-    {
-        // k = part*64 + ri*32 + a: K-block ab (re hi), 4+ab (im hi), 8+ab (re lo), 12+ab (im lo)
-        unsigned char *arow = Asm + core_off(w * 32 + l, 0, SP_A_LBO);
-#pragma unroll
-        for (int ab = 0; ab < 4; ab++) {
-            uint4 hr, hi, lr, li;
-            uint32_t *phr = &hr.x, *phi = &hi.x, *plr = &lr.x, *pli = &li.x;
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const float2 e0 = v[ab * 8 + 2 * q], e1 = v[ab * 8 + 2 * q + 1];
-                split2<BF>(e0.x * s1, e1.x * s1, phr[q], plr[q]);
-                split2<BF>(e0.y * s1, e1.y * s1, phi[q], pli[q]);
-            }
-            *reinterpret_cast<uint4 *>(arow + (0 + ab) * SP_A_LBO) = hr;
-            *reinterpret_cast<uint4 *>(arow + (4 + ab) * SP_A_LBO) = hi;
-            *reinterpret_cast<uint4 *>(arow + (8 + ab) * SP_A_LBO) = lr;
-            *reinterpret_cast<uint4 *>(arow + (12 + ab) * SP_A_LBO) = li;
-        }
-    }
-    tc::fence_async_smem();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tbase = tslot;
-    const uint32_t idesc = tc::idesc_f16(SPM, SPNN, BF ? 1 : 0);
-    const uint32_t a0 = tc::smem_addr(Asm), b0 = tc::smem_addr(Bsm);
-    if (tid == 0) {
-        split_mma(tbase, a0, b0, idesc);
-        tc::mma_commit(&mbar);
-    }
-    bool ok = tc::mbar_wait(&mbar, 0, SP_WAIT_LIMIT);
-    ok = __syncthreads_and(ok);
-    uint32_t pending = ok ? 2u : 0u;  // phase still outstanding if a wait gives up
-    tc::fence_after_sync();
-    // ---- step 1 result: lane (w, l) = (row, b), columns re c | im c
-    float zr[32], zi[32];
-    const uint32_t lane_base = tbase + ((uint32_t)(w * 32) << 16);
-    if (ok) {
-        tmem_ld32(lane_base + 0, zr);
-        tmem_ld32(lane_base + 32, zi);
-        tc::tmem_ld_wait();
-    }
-    // twiddle w1024^(b c), b = l: table row c is contiguous over b
-    mx = 0.f;
-#pragma unroll
-    for (int c = 0; c < 32; c++) {
-        const float2 t = __ldg(&a.tw[c * 32 + l]);
-        const float r = zr[c] * t.x - zi[c] * t.y, i = zr[c] * t.y + zi[c] * t.x;
-        zr[c] = r;
-        zi[c] = i;
-        mx = fmaxf(mx, fmaxf(fabsf(r), fabsf(i)));
-    }
-    const float s2 = BF ? 1.f : warp_scale(mx);
-    // ---- step 2 operand: A2[(w, c)][part*64 + ri*32 + b], b = l, written over
-    // step 1's operand.  Lane pairs (l, l^1) trade one word so that each lane
-    // stores two 4-byte pairs of adjacent b: even lanes (re hi, im hi) at b = l,
-    // odd lanes (re lo, im lo) at b = l - 1.  The two stores are ordered so the
-    // even and odd halves of the warp fall in different banks.
-    {
-        const bool even = (l & 1) == 0;
-        const int k1 = even ? l : 96 + l - 1, k2 = even ? 32 + l : 64 + l - 1;
-        unsigned char *p1 = Asm + core_off(w * 32, k1, SP_A_LBO);
-        unsigned char *p2 = Asm + core_off(w * 32, k2, SP_A_LBO);
-#pragma unroll
-        for (int c = 0; c < 32; c++) {
-            uint32_t P, Q;  // (re hi | im hi << 16), (re lo | im lo << 16)
-            split2<BF>(zr[c] * s2, zi[c] * s2, P, Q);
-            const uint32_t R = __shfl_xor_sync(0xffffffffu, even ? Q : P, 1);
-            const uint32_t X = even ? P : R, Y = even ? R : Q;
-            const uint32_t wlo = __byte_perm(X, Y, 0x5410), whi = __byte_perm(X, Y, 0x7632);
-            const uint32_t mo = (uint32_t)((c >> 3) << 7) + (uint32_t)((c & 7) << 4);
-            *reinterpret_cast<uint32_t *>(p1 + mo) = even ? wlo : whi;
-            *reinterpret_cast<uint32_t *>(p2 + mo) = even ? whi : wlo;
-        }
-    }
-    // the step 1 accumulator is read out: step 2 reuses its columns
-    tc::fence_async_smem();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    if (tid == 0 && ok) {
-        split_mma(tbase, a0, b0, idesc);
-        tc::mma_commit(&mbar);
-    }
-    if (ok) {
-        ok = tc::mbar_wait(&mbar, 1, SP_WAIT_LIMIT);
-        ok = __syncthreads_and(ok);
-        pending = ok ? 2u : 1u;
-    }
-    tc::fence_after_sync();
-    // ---- step 2 result: lane (w, l) = (row, c = l), columns re d | im d -> out[c + 32 d]
-    if (ok) {
-        float yr[32], yi[32];
-        tmem_ld32(lane_base + 0, yr);
-        tmem_ld32(lane_base + 32, yi);
-        tc::tmem_ld_wait();
-        if (live) {
-            const float f = (a.has_scale ? a.scale : 1.f) / (s1 * s2);
-            float2 *dst = a.out + a.off_out + row * a.vs_out;
-#pragma unroll
-            for (int d = 0; d < 32; d++) {
-                float2 o = make_float2(yr[d] * f, yi[d] * f);
-                if (a.inv) o.y = -o.y;
-                dst[l + 32 * d] = o;
-            }
-        }
-    } else {
+    uint32_t pending = 2u;
+    const bool ok = sp_group<BF>(a, Asm, tc::smem_addr(Asm), tc::smem_addr(Bsm), tslot, &mbar, v, row, tid, &pending);
+    if (!ok) {
         if (tid == 0) atomicExch(a.status, 1);
         // let MMAs still in flight finish (bounded) before the tensor memory is freed
         if (pending < 2u) tc::mbar_wait(&mbar, pending, SP_WAIT_LIMIT);
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (w == 0) tc::tmem_dealloc(tbase, SP_TMEM_COLS);
+    if (w == 0) tc::tmem_dealloc(tslot, SP_TMEM_COLS);
 }
 
 // ---------------------------------------------------------------- host side
@@ -374,6 +406,7 @@ bool launch_split_f32(const Job &j, cudaStream_t st) {
     // operand reads: A chunks start at 2 * ka * SP_A_LBO (ka < 8) and span two
     // K-blocks of 16 x 128 bytes, ending at byte 16 * SP_A_LBO - 17 of A; B
     // chunks end at byte 16 * SP_B_LBO - 1 of B: both inside their operands
+    const long ngroups = (j.nvec + 3) / 4;
     const size_t smem = SP_A_BYTES + SP_B_BYTES;
     static bool attr[2] = {false, false};
     if (!attr[bf]) {
@@ -382,9 +415,8 @@ bool launch_split_f32(const Job &j, cudaStream_t st) {
         if (!cuda_ok(e, "cudaFuncSetAttribute")) return true;
         attr[bf] = true;
     }
-    const long grid = (j.nvec + 3) / 4;
-    if (bf) k_split1024<true><<<(unsigned)grid, 128, smem, st>>>(a);
-    else k_split1024<false><<<(unsigned)grid, 128, smem, st>>>(a);
+    if (bf) k_split1024<true><<<(unsigned)ngroups, 128, smem, st>>>(a);
+    else k_split1024<false><<<(unsigned)ngroups, 128, smem, st>>>(a);
     count_launch();
     cuda_ok(cudaGetLastError(), "k_split1024 launch");
     return true;

@@ -70,3 +70,59 @@ def test_split_form_in_place_and_fallback():
     ys = np.zeros_like(xs)
     q.ccfftmop(J.CBlock(xs).view(0, 512, 8, 1, 512), J.CBlock(ys).view(0, 512, 8, 1, 512))
     assert np.isfinite(ys).all() and np.abs(ys).max() > 0
+
+
+def scaled_rows(Mr, seed):
+    g = np.random.default_rng(seed)
+    z = g.standard_normal((Mr, N)) + 1j * g.standard_normal((Mr, N))
+    return z * (10.0 ** g.uniform(-3, 3, Mr))[:, None]
+
+
+def rows_worst(got, ref):
+    return float(np.max(np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)))
+
+
+@pytest.mark.parametrize("form,bound", [(J.JVSIP_FORM_SPLIT_FP16, 1e-6), (J.JVSIP_FORM_SPLIT_BF16, 1e-5)],
+                         ids=["fp16", "bf16"])
+def test_split_form_many_groups(form, bound):
+    # several waves of 4-row groups (2434 CTAs) and a last group of 2 rows,
+    # forward and inverse
+    Mr = 2 * 152 * 4 * 3 + 2
+    z = scaled_rows(Mr, 41)
+    x = np.empty(2 * Mr * N, np.float32)
+    x[0::2], x[1::2] = z.real.reshape(-1), z.imag.reshape(-1)
+    y = np.zeros_like(x)
+    bx, by = J.CBlock(x, admit=True), J.CBlock(y, admit=True, update=False)
+    for d in (-1, 1):
+        p = J.FFTM(J.KIND_CCOP, Mr, N, 1.0, d, J.VSIP_ROW)
+        p.setform(form)
+        p.ccfftmop(bx.view(0, N, Mr, 1, N), by.view(0, N, Mr, 1, N))
+        assert J.lib().jvsip_gpu_synchronize() == 0, J.last_error()
+        by.sync()
+        got = (y[0::2] + 1j * y[1::2].astype(np.float64)).reshape(Mr, N)
+        ref = np.fft.fft(z, axis=1) if d == -1 else np.fft.ifft(z, axis=1) * N
+        assert rows_worst(got, ref) <= bound
+
+
+def test_split_form_unaligned_rows():
+    # rows starting 8 bytes off a 16-byte boundary (odd offset and pitch), in
+    # place, with a scale
+    Mr, pitch, off = 37, N + 1, 1
+    z = scaled_rows(Mr, 43)
+    buf = np.zeros((off + Mr * pitch), np.complex128)
+    for r in range(Mr):
+        buf[off + r * pitch: off + r * pitch + N] = z[r]
+    x = np.empty(2 * buf.size, np.float32)
+    x[0::2], x[1::2] = buf.real, buf.imag
+    bx = J.CBlock(x, admit=True)
+    p = J.FFTM(J.KIND_CCIP, Mr, N, 0.5, -1, J.VSIP_ROW)
+    p.setform(J.JVSIP_FORM_SPLIT_FP16)
+    p.ccfftmip(bx.view(off, pitch, Mr, 1, N))
+    assert J.lib().jvsip_gpu_synchronize() == 0, J.last_error()
+    bx.release(True)
+    c = x[0::2] + 1j * x[1::2].astype(np.float64)
+    got = np.stack([c[off + r * pitch: off + r * pitch + N] for r in range(Mr)])
+    assert rows_worst(got, 0.5 * np.fft.fft(z, axis=1)) <= 1e-6
+    # the gaps between rows keep their (zero) values
+    for r in range(Mr - 1):
+        assert c[off + r * pitch + N] == 0
