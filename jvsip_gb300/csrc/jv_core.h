@@ -183,6 +183,8 @@ bool launch_global_f32(const Job &j, cudaStream_t s);
 bool launch_global_f64(const Job &j, cudaStream_t s);
 bool launch_fast_f32(const Job &j, cudaStream_t s);   // specialised kernels; false when none fits
 bool launch_fast_real_f32(const Job &j, cudaStream_t s);  // R2C / C2R rows on the specialised kernel
+bool launch_fast_komega_r2c_f32(const Job &j, cudaStream_t s);    // k-omega tapered R2C rows (specialised kernel)
+bool launch_fast_komega_power_f32(const Job &j, cudaStream_t s);  // k-omega power columns (specialised kernel)
 std::vector<int> fast_radices(long N);                // radix list of the specialised kernel for N
 bool fast_step_len(long N);                           // lengths the specialised kernel takes as long-transform steps
 bool launch_fast_step_f32(const Job &j, cudaStream_t s);  // a long-transform step in column-tile mode (single group)

@@ -39,19 +39,19 @@ std::vector<int> fast_radices(long N) {
 }
 
 // Rows: T threads per transform, RPC transforms per CTA.
-template <bool SPLIT>
+template <bool SPLIT, int FXK = 0>
 static bool launch_fast_rows(const Job &j, cudaStream_t st) {
     switch (j.N) {
-        case 64: return launch_fast_n<64, 4, 64, RList<16, 4>, SPLIT, false>(j, st);
-        case 128: return launch_fast_n<128, 8, 32, RList<16, 8>, SPLIT, false>(j, st);
-        case 256: return launch_fast_n<256, 16, 16, RList<16, 16>, SPLIT, false>(j, st);
-        case 512: return launch_fast_n<512, 32, 8, RList<16, 16, 2>, SPLIT, false>(j, st);
-        case 768: return launch_fast_n<768, 32, 4, RList<12, 8, 8>, SPLIT, false>(j, st);
-        case 1000: return launch_fast_n<1000, 100, 4, RList<10, 10, 10>, SPLIT, false>(j, st);
-        case 1024: return launch_fast_n<1024, 64, 4, RList<16, 16, 4>, SPLIT, false>(j, st);
-        case 2048: return launch_fast_n<2048, 128, 2, RList<16, 16, 8>, SPLIT, false>(j, st);
-        case 4096: return launch_fast_n<4096, 256, 1, RList<16, 16, 16>, SPLIT, false>(j, st);
-        case 8192: return launch_fast_n<8192, 512, 1, RList<16, 16, 16, 2>, SPLIT, false>(j, st);
+        case 64: return launch_fast_n<64, 4, 64, RList<16, 4>, SPLIT, false, false, false, 0, FXK>(j, st);
+        case 128: return launch_fast_n<128, 8, 32, RList<16, 8>, SPLIT, false, false, false, 0, FXK>(j, st);
+        case 256: return launch_fast_n<256, 16, 16, RList<16, 16>, SPLIT, false, false, false, 0, FXK>(j, st);
+        case 512: return launch_fast_n<512, 32, 8, RList<16, 16, 2>, SPLIT, false, false, false, 0, FXK>(j, st);
+        case 768: return launch_fast_n<768, 32, 4, RList<12, 8, 8>, SPLIT, false, false, false, 0, FXK>(j, st);
+        case 1000: return launch_fast_n<1000, 100, 4, RList<10, 10, 10>, SPLIT, false, false, false, 0, FXK>(j, st);
+        case 1024: return launch_fast_n<1024, 64, 4, RList<16, 16, 4>, SPLIT, false, false, false, 0, FXK>(j, st);
+        case 2048: return launch_fast_n<2048, 128, 2, RList<16, 16, 8>, SPLIT, false, false, false, 0, FXK>(j, st);
+        case 4096: return launch_fast_n<4096, 256, 1, RList<16, 16, 16>, SPLIT, false, false, false, 0, FXK>(j, st);
+        case 8192: return launch_fast_n<8192, 512, 1, RList<16, 16, 16, 2>, SPLIT, false, false, false, 0, FXK>(j, st);
         default: return false;
     }
 }
@@ -63,20 +63,20 @@ static bool launch_fast_rows(const Job &j, cudaStream_t st) {
 // 2927 (2472), 2048: 2059 (2000), 1000 x 4096: 2054 (1785).  1000 points take
 // 4 columns per CTA, 2 CTAs per SM: 29.6 us on 1000 x 4096 against 31.4 us
 // for 8 columns per CTA (one CTA per SM) and 40.9 us for 2.
-template <bool SPLIT>
+template <bool SPLIT, int FXK = 0>
 static bool launch_fast_cols(const Job &j, cudaStream_t st) {
     switch (j.N) {
-        case 64: return launch_fast_n<64, 4, 64, RList<16, 4>, SPLIT, true>(j, st);
-        case 128: return launch_fast_n<128, 8, 32, RList<16, 8>, SPLIT, true>(j, st);
-        case 256: return launch_fast_n<256, 16, 16, RList<16, 16>, SPLIT, true>(j, st);
-        case 512: return launch_fast_n<512, 32, 16, RList<16, 16, 2>, SPLIT, true>(j, st);
-        case 1000: return launch_fast_n<1000, 100, 4, RList<10, 10, 10>, SPLIT, true>(j, st);
-        case 1024: return launch_fast_n<1024, 64, 8, RList<16, 16, 4>, SPLIT, true>(j, st);
-        case 2048: return launch_fast_n<2048, 128, 4, RList<16, 16, 8>, SPLIT, true>(j, st);
+        case 64: return launch_fast_n<64, 4, 64, RList<16, 4>, SPLIT, true, false, false, 0, FXK>(j, st);
+        case 128: return launch_fast_n<128, 8, 32, RList<16, 8>, SPLIT, true, false, false, 0, FXK>(j, st);
+        case 256: return launch_fast_n<256, 16, 16, RList<16, 16>, SPLIT, true, false, false, 0, FXK>(j, st);
+        case 512: return launch_fast_n<512, 32, 16, RList<16, 16, 2>, SPLIT, true, false, false, 0, FXK>(j, st);
+        case 1000: return launch_fast_n<1000, 100, 4, RList<10, 10, 10>, SPLIT, true, false, false, 0, FXK>(j, st);
+        case 1024: return launch_fast_n<1024, 64, 8, RList<16, 16, 4>, SPLIT, true, false, false, 0, FXK>(j, st);
+        case 2048: return launch_fast_n<2048, 128, 4, RList<16, 16, 8>, SPLIT, true, false, false, 0, FXK>(j, st);
         // 4096 points: 4 columns per 1024-thread CTA (139 KB of shared memory),
         // 2874 GB/s on 4096 x 4096 against 1807 for 2 columns per CTA and 1823
         // for the shared-memory kernel
-        case 4096: return launch_fast_n<4096, 256, 4, RList<16, 16, 16>, SPLIT, true>(j, st);
+        case 4096: return launch_fast_n<4096, 256, 4, RList<16, 16, 16>, SPLIT, true, false, false, 0, FXK>(j, st);
         default: return false;
     }
 }
@@ -128,6 +128,27 @@ bool launch_fast_sp_f32(const Job &j, cudaStream_t st) {
         case 4096: return launch_fast_n<4096, 256, 2, RList<16, 16, 16>, false, true, false, true>(j, st);
         default: return false;
     }
+}
+
+// The k-omega pipeline's c2c transforms down the spectrum's columns: the last
+// pass stores (p, Im X) with p = s|X|^2 and adds p to the gram (kw.c's
+// vsip_mcmagsq_f, vsip_smmul_f, vsip_madd_f).  Interleaved views: contiguous
+// transforms (a column-major spectrum, as kw.c creates it) on the row
+// mapping, adjacent transforms (a row-major one) as column tiles.
+bool launch_fast_komega_power_f32(const Job &j, cudaStream_t st) {
+    if (j.prec != P_F32 || j.kind != K_C2C || !j.gram || !j.twp || j.lp || j.nbatch > 1 || j.tw_lo) return false;
+    const CView &ci = j.cin, &co = j.cout;
+    if (ci.cst != 2 || co.cst != 2 || (const float *)ci.im != (const float *)ci.re + 1 ||
+        (const float *)co.im != (const float *)co.re + 1 || ((uintptr_t)ci.re % 8) || ((uintptr_t)co.re % 8))
+        return false;
+    if (j.nvec <= 0 || j.nvec > 0x7fffffffL) return false;
+    if (ci.es == 1 && co.es == 1) {
+        if (j.nvec > 1 && (labs(ci.vs) < j.N || labs(co.vs) < j.N)) return false;
+        return launch_fast_rows<false, FX_POWER>(j, st);
+    }
+    if (j.nvec < 16 || labs(ci.vs) != 1 || labs(co.vs) != 1) return false;
+    if (labs(ci.es) < j.nvec || labs(co.es) < j.nvec) return false;
+    return launch_fast_cols<false, FX_POWER>(j, st);
 }
 
 // Specialised kernels: rows of unit element stride, or column tiles

@@ -81,6 +81,16 @@ struct FastArgs {
     float scale;
     const float2 *twp; // per-pass twiddles: pass p at its offset, entry r*Ns + m = exp(-2 pi i r m/(Ns R))
     const float2 *thalf; // real rows: exp(-+ i pi k/N), k <= N (R2C: minus, C2R: plus)
+    // k-omega fusions (FXK): FX_TAPER -- real pair n of row v times (ts[2n],
+    // ts[2n+1]) then arr[v], each product rounded, written back to the row
+    // through wb; FX_POWER -- output k of transform v stored as (p, Im X) with
+    // p = g_scale |X|^2, and p added to gram[v*g_vs + k*g_es]
+    const float *tp_n, *tp_t;
+    long tp_n_st, tp_t_st;
+    float2 *wb;
+    float *gram;
+    long g_es, g_vs;
+    float g_scale;
 };
 
 // twiddle and DFT of the thread's E/R butterflies of a radix-R pass; the
@@ -127,7 +137,9 @@ __device__ __forceinline__ void store_pass(const float2 (&v)[E], float2 *s, int 
 // k = 0..N (Z_N = Z_0; w_k = exp(-i pi k/N)), the scale applied to Z first as
 // the reference does (VI_rcfftmop_f_def.h:79-118).  The thread of pair
 // (k, N-k), k = t + T*i <= N/2, reads Z_k and Z_{N-k} once and writes X_k and
-// X_{N-k} (X_N for k = 0): ascending and descending coalesced stores.
+// X_{N-k} (X_N for k = 0): ascending and descending coalesced stores when the
+// output rows are contiguous; output element k at k*es_out (column-major
+// spectra: adjacent rows' X_k are adjacent).
 template <int N, int T, int E, int R>
 __device__ __forceinline__ void r2c_finish(const float2 (&v)[E], float2 *s, int t, const FastArgs &a, long row,
                                            bool live, int Ns) {
@@ -154,20 +166,22 @@ __device__ __forceinline__ void r2c_finish(const float2 (&v)[E], float2 *s, int 
             zn = cscale(zn, a.scale);
         }
         const float2 w = __ldg(&a.thalf[k]), w2 = __ldg(&a.thalf[nk]);
-        o[k] = make_float2(0.5f * (zn.x + zk.x + w.x * (zn.y + zk.y) + w.y * (zk.x - zn.x)),
-                           0.5f * (zk.y - zn.y + w.x * (zn.x - zk.x) + w.y * (zn.y + zk.y)));
+        o[k * a.es_out] = make_float2(0.5f * (zn.x + zk.x + w.x * (zn.y + zk.y) + w.y * (zk.x - zn.x)),
+                                      0.5f * (zk.y - zn.y + w.x * (zn.x - zk.x) + w.y * (zn.y + zk.y)));
         if (nk != k)
-            o[nk] = make_float2(0.5f * (zk.x + zn.x + w2.x * (zk.y + zn.y) + w2.y * (zn.x - zk.x)),
-                                0.5f * (zn.y - zk.y + w2.x * (zk.x - zn.x) + w2.y * (zk.y + zn.y)));
+            o[nk * a.es_out] = make_float2(0.5f * (zk.x + zn.x + w2.x * (zk.y + zn.y) + w2.y * (zn.x - zk.x)),
+                                           0.5f * (zn.y - zk.y + w2.x * (zk.x - zn.x) + w2.y * (zk.y + zn.y)));
     }
 }
 
 // Passes after the first.  On entry shared memory holds the previous pass's output.
-template <int N, int T, int E, int NsIn, int Off, typename L, bool SPLIT, bool COLS, bool TW, bool SP, int RM>
+template <int N, int T, int E, int NsIn, int Off, typename L, bool SPLIT, bool COLS, bool TW, bool SP, int RM,
+          int FXK>
 struct Passes;
 
-template <int N, int T, int E, int NsIn, int Off, int R0, int... Rs, bool SPLIT, bool COLS, bool TW, bool SP, int RM>
-struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>, SPLIT, COLS, TW, SP, RM> {
+template <int N, int T, int E, int NsIn, int Off, int R0, int... Rs, bool SPLIT, bool COLS, bool TW, bool SP, int RM,
+          int FXK>
+struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>, SPLIT, COLS, TW, SP, RM, FXK> {
     static __device__ __forceinline__ void run(float2 (&v)[E], float2 *s, int t, const FastArgs &a, long row,
                                                bool live) {
         __syncthreads();
@@ -203,6 +217,15 @@ struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>, SPLIT, COLS, TW, SP, RM> {
                         if (a.inv) c.y = -c.y;
                         if (a.has_scale) c = cscale(c, a.scale);
                         const int k = j + r * NsIn;
+                        if constexpr ((FXK & FX_POWER) != 0) {
+                            // p = |X|^2 (vsip_mcmagsq_f), p *= s (vsip_smmul_f),
+                            // gram = p + gram (vsip_madd_f), rounded in that order
+                            float p = add_rn(mul_rn(c.x, c.x), mul_rn(c.y, c.y));
+                            p = mul_rn(a.g_scale, p);
+                            float *g = a.gram + row * a.g_vs + (long)k * a.g_es;
+                            *g = add_rn(p, *g);
+                            c.x = p;
+                        }
                         if constexpr (COLS) {
                             const long e = (long)k * ks;
                             if constexpr (SPLIT) {
@@ -225,8 +248,8 @@ struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>, SPLIT, COLS, TW, SP, RM> {
         } else {
             __syncthreads();
             store_pass<N, T, E, R0>(v, s, t, NsIn);
-            Passes<N, T, E, NsIn * R0, Off + R0 * NsIn, RList<Rs...>, SPLIT, COLS, TW, SP, RM>::run(v, s, t, a, row,
-                                                                                                 live);
+            Passes<N, T, E, NsIn * R0, Off + R0 * NsIn, RList<Rs...>, SPLIT, COLS, TW, SP, RM, FXK>::run(v, s, t, a,
+                                                                                                      row, live);
         }
     }
 };
@@ -249,7 +272,7 @@ constexpr int fast_min_blocks() {
     return (T * RPC <= 512 && !SP) ? ((N / T > 16) ? 896 : 1024) / (T * RPC) : 1;
 }
 
-template <int N, int T, int RPC, typename L, bool SPLIT, bool COLS, bool TW, bool SP, int RM>
+template <int N, int T, int RPC, typename L, bool SPLIT, bool COLS, bool TW, bool SP, int RM, int FXK>
 __global__ void __launch_bounds__(T *RPC, fast_min_blocks<N, T, RPC, SP>()) k_fast(const FastArgs pa) {
     constexpr int E = N / T;
     constexpr int R1 = L::first;
@@ -292,6 +315,13 @@ __global__ void __launch_bounds__(T *RPC, fast_min_blocks<N, T, RPC, SP>()) k_fa
                 if constexpr (SPLIT) c = make_float2(inr[n], ini[n]);
                 else c = inb[n];
             }
+            if constexpr (RM == 1 && (FXK & FX_TAPER) != 0) {
+                // kw.c: data = ts * data (VSIP_ROW), then data = arr * data (VSIP_COL)
+                const float wt = a.tp_t[rowc * a.tp_t_st];
+                c.x = mul_rn(mul_rn(a.tp_n[2L * n * a.tp_n_st], c.x), wt);
+                c.y = mul_rn(mul_rn(a.tp_n[(2L * n + 1) * a.tp_n_st], c.y), wt);
+                if (live) a.wb[ib + n] = c;
+            }
             if (a.inv) c.y = -c.y;
             if constexpr (SP) {
                 // Stockham input twiddle W_Nt^(n*m*stride), n = element index
@@ -315,15 +345,16 @@ __global__ void __launch_bounds__(T *RPC, fast_min_blocks<N, T, RPC, SP>()) k_fa
             const int t2 = (int)threadIdx.x % T, rl2 = (int)threadIdx.x / T;
             const long row2 = (long)blockIdx.x * RPC + rl2;
             const bool live2 = row2 < a.nvec;
-            Passes<N, T, E, R1, R1, typename L::rest, SPLIT, COLS, TW, SP, RM>::run(
+            Passes<N, T, E, R1, R1, typename L::rest, SPLIT, COLS, TW, SP, RM, FXK>::run(
                 v, reinterpret_cast<float2 *>(smem_raw) + rl2 * NP, t2, a, live2 ? row2 : a.nvec - 1, live2);
             return;
         }
     }
-    Passes<N, T, E, R1, R1, typename L::rest, SPLIT, COLS, TW, SP, RM>::run(v, s, t, a, rowc, live);
+    Passes<N, T, E, R1, R1, typename L::rest, SPLIT, COLS, TW, SP, RM, FXK>::run(v, s, t, a, rowc, live);
 }
 
-template <int N, int T, int RPC, typename L, bool SPLIT, bool COLS, bool TW = false, bool SP = false, int RM = 0>
+template <int N, int T, int RPC, typename L, bool SPLIT, bool COLS, bool TW = false, bool SP = false, int RM = 0,
+          int FXK = 0>
 static bool launch_fast_n(const Job &j, cudaStream_t st) {
     FastArgs a;
     a.sp_ns = j.sp_ns;
@@ -367,20 +398,31 @@ static bool launch_fast_n(const Job &j, cudaStream_t st) {
         a.es_out = 1;
         a.inv = 1;
     }
+    a.tp_n = (const float *)j.taper_n;
+    a.tp_t = (const float *)j.taper_t;
+    a.tp_n_st = j.taper_n_st;
+    a.tp_t_st = j.taper_t_st;
+    a.wb = const_cast<float2 *>(a.in);
+    a.gram = (float *)j.gram;
+    a.g_es = j.gram_es;
+    a.g_vs = j.gram_vs;
+    a.g_scale = (float)j.gram_scale;
     if (!a.twp || (RM != 0 && !a.thalf)) return false;
+    if ((FXK & FX_TAPER) != 0 && (!a.tp_n || !a.tp_t || !j.taper_back)) return false;
+    if ((FXK & FX_POWER) != 0 && !a.gram) return false;
     constexpr int NP = fast_pitch<N, RPC, COLS>();
     size_t smem = (size_t)RPC * NP * sizeof(float2);
     static bool attr = false;
     if (!attr) {
         if (smem > 48 * 1024 &&
-            !cuda_ok(cudaFuncSetAttribute(k_fast<N, T, RPC, L, SPLIT, COLS, TW, SP, RM>,
+            !cuda_ok(cudaFuncSetAttribute(k_fast<N, T, RPC, L, SPLIT, COLS, TW, SP, RM, FXK>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                      "cudaFuncSetAttribute"))
             return false;
         attr = true;
     }
     long grid = (j.nvec + RPC - 1) / RPC;
-    k_fast<N, T, RPC, L, SPLIT, COLS, TW, SP, RM><<<(unsigned)grid, T * RPC, smem, st>>>(a);
+    k_fast<N, T, RPC, L, SPLIT, COLS, TW, SP, RM, FXK><<<(unsigned)grid, T * RPC, smem, st>>>(a);
     count_launch();
     return cuda_ok(cudaGetLastError(), "k_fast launch");
 }

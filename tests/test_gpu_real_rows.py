@@ -141,3 +141,27 @@ def test_c2c_rows_768():
         v.destroy()
     bx.destroy()
     by.destroy()
+
+
+@pytest.mark.parametrize("H", [256, 768, 2048])
+def test_r2c_rows_into_column_major_spectrum(H):
+    # real rows in, the spectrum stored column-major (element stride M,
+    # adjacent rows' bins adjacent), as kw.c lays out its frequency matrix
+    N, M = 2 * H, 24
+    g = np.random.default_rng(H + 5)
+    xr = g.standard_normal((M, N))
+    x = xr.astype(np.float32).reshape(-1).copy()
+    z = np.zeros(2 * M * (H + 1), np.float32)
+    bx, bz = J.RBlock(x), J.CBlock(z)
+    bx.admit(True)
+    bz.admit(False)
+    vx, vz = bx.view(0, N, M, 1, N), bz.view(0, 1, M, M, H + 1)
+    J.FFTM(J.KIND_RCOP, M, N, 1.0, J.VSIP_FFT_FWD, J.VSIP_ROW).rcfftmop(vx, vz)
+    J.check("r2c column-major")
+    bz.sync()
+    got = cplx(z).reshape(H + 1, M).T
+    assert rel(got, np.fft.rfft(xr, axis=1)) <= tol(N)
+    for v in (vx, vz):
+        v.destroy()
+    bx.destroy()
+    bz.destroy()
