@@ -64,6 +64,7 @@ struct SplitArgs {
     const uint4 *bop;     // B operand, SP_B_BYTES in core-matrix layout
     const float2 *tw;     // [c][b] = exp(-2 pi i bc/1024), c, b < 32
     int *status;          // set to 1 when a barrier wait expired
+    int bulk_rows;        // rows start on 16-byte boundaries: loaded by bulk copies
 };
 
 // two floats -> one 32-bit word of two 16-bit values (first in the low half),
@@ -210,13 +211,6 @@ __device__ __forceinline__ void sp_store(const SplitArgs &a, uint32_t lane_base,
     }
 }
 
-// B operand (constant per plan) into shared memory
-__device__ __forceinline__ void sp_load_b(unsigned char *Bsm, const uint4 *__restrict__ bop, int tid) {
-    uint4 *dst = reinterpret_cast<uint4 *>(Bsm);
-#pragma unroll
-    for (int i = 0; i < SP_B_BYTES / 16 / 128; i++) dst[tid + 128 * i] = __ldg(&bop[tid + 128 * i]);
-}
-
 // Steps 1 and 2 of the group whose rows the threads hold in v (conjugated when
 // inverse): operand, MMAs, twiddle, operand, MMAs, store.  Returns false when
 // a barrier wait expired (uniform over the CTA); *pending is then the MMA
@@ -277,31 +271,61 @@ __global__ void __launch_bounds__(128, 4) k_split1024(const SplitArgs a) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *Bsm = smem;                     // 16 KiB
     unsigned char *Asm = smem + SP_B_BYTES;        // 33024 bytes
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar, bbar, ibar;
     __shared__ uint32_t tslot;
     const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
-    const long row = (long)blockIdx.x * 4 + w;
+    const long row0 = (long)blockIdx.x * 4, row = row0 + w;
     const bool live = row < a.nvec;
+    const int nr = (int)min(4L, a.nvec - row0);
     if (w == 0) {
         tc::tmem_alloc(&tslot, SP_TMEM_COLS);
         tc::tmem_relinquish();
     }
-    if (tid == 0) tc::mbar_init(&mbar, 1);
-    sp_load_b(Bsm, a.bop, tid);
+    if (tid == 0) {
+        tc::mbar_init(&mbar, 1);
+        // the B operand (constant per plan) by one bulk copy, and with rows on
+        // 16-byte boundaries the group's rows by one bulk copy each into the A
+        // operand's space (free until step 1's operand is written)
+        tc::mbar_init(&bbar, 1);
+        tc::mbar_expect_tx(&bbar, SP_B_BYTES);
+        tc::bulk_load(Bsm, a.bop, SP_B_BYTES, &bbar);
+        if (a.bulk_rows) {
+            tc::mbar_init(&ibar, 1);
+            tc::mbar_expect_tx(&ibar, (uint32_t)(nr * SPN * 8));
+            for (int r = 0; r < nr; r++)
+                tc::bulk_load(Asm + r * SPN * 8, a.in + a.off_in + (row0 + r) * a.vs_in, SPN * 8, &ibar);
+        }
+    }
     // thread (w, l) owns vector b = l of row w: x[32a + l], a < 32
     float2 v[32];
-    const float2 *src = a.in + a.off_in + (live ? row : 0) * a.vs_in;
+    bool ok = true;
+    if (a.bulk_rows) {
+        __syncthreads();  // the barrier is initialised
+        ok = tc::mbar_wait(&ibar, 0, SP_WAIT_LIMIT);
+        const float2 *src = reinterpret_cast<const float2 *>(Asm) + w * SPN;
 #pragma unroll
-    for (int i = 0; i < 32; i++) {
-        float2 c = live ? src[32 * i + l] : make_float2(0.f, 0.f);
-        if (a.inv) c.y = -c.y;
-        v[i] = c;
+        for (int i = 0; i < 32; i++) {
+            float2 c = (live && ok) ? src[32 * i + l] : make_float2(0.f, 0.f);
+            if (a.inv) c.y = -c.y;
+            v[i] = c;
+        }
+    } else {
+        const float2 *src = a.in + a.off_in + (live ? row : 0) * a.vs_in;
+#pragma unroll
+        for (int i = 0; i < 32; i++) {
+            float2 c = live ? src[32 * i + l] : make_float2(0.f, 0.f);
+            if (a.inv) c.y = -c.y;
+            v[i] = c;
+        }
     }
     tc::fence_before_sync();
-    __syncthreads();
+    ok = __syncthreads_and(ok);  // also: every thread has read its row from the A space
     tc::fence_after_sync();
     uint32_t pending = 2u;
-    const bool ok = sp_group<BF>(a, Asm, tc::smem_addr(Asm), tc::smem_addr(Bsm), tslot, &mbar, v, row, tid, &pending);
+    if (!ok && a.bulk_rows) tc::mbar_wait(&ibar, 0, SP_WAIT_LIMIT);
+    ok = ok && __syncthreads_and(tc::mbar_wait(&bbar, 0, SP_WAIT_LIMIT));
+    if (ok) ok = sp_group<BF>(a, Asm, tc::smem_addr(Asm), tc::smem_addr(Bsm), tslot, &mbar, v, row, tid, &pending);
+    else tc::mbar_wait(&bbar, 0, SP_WAIT_LIMIT);  // the copy ends before the CTA's shared memory is released
     if (!ok) {
         if (tid == 0) atomicExch(a.status, 1);
         // let MMAs still in flight finish (bounded) before the tensor memory is freed
@@ -407,6 +431,7 @@ bool launch_split_f32(const Job &j, cudaStream_t st) {
     // K-blocks of 16 x 128 bytes, ending at byte 16 * SP_A_LBO - 17 of A; B
     // chunks end at byte 16 * SP_B_LBO - 1 of B: both inside their operands
     const long ngroups = (j.nvec + 3) / 4;
+    a.bulk_rows = ((uintptr_t)ci.re % 16) == 0 && (ci.off % 2) == 0 && (j.nvec == 1 || (ci.vs % 2) == 0);
     const size_t smem = SP_A_BYTES + SP_B_BYTES;
     static bool attr[2] = {false, false};
     if (!attr[bf]) {

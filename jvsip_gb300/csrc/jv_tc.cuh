@@ -113,6 +113,13 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const void *tmap, int x, 
         :: "r"(smem_addr(dst)), "l"(tmap), "r"(x), "r"(y), "r"(smem_addr(mbar)) : "memory");
 }
 
+// 1-D bulk copy of `bytes` (a multiple of 16) from global to shared memory,
+// both addresses 16-byte aligned, completing `bytes` transactions on the barrier
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, void *mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(mbar)) : "memory");
+}
+
 // 32 lanes x 32 bits, 16 consecutive columns per thread
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     uint32_t r[16];
