@@ -64,7 +64,8 @@ struct SplitArgs {
     const uint4 *bop;     // B operand, SP_B_BYTES in core-matrix layout
     const float2 *tw;     // [c][b] = exp(-2 pi i bc/1024), c, b < 32
     int *status;          // set to 1 when a barrier wait expired
-    int bulk_rows;        // rows start on 16-byte boundaries: loaded by bulk copies
+    int bulk_rows;        // input rows start on 16-byte boundaries: loaded by bulk copies
+    int bulk_out;         // output rows start on 16-byte boundaries: stored by bulk copies
 };
 
 // two floats -> one 32-bit word of two 16-bit values (first in the low half),
@@ -195,11 +196,37 @@ __device__ __forceinline__ float sp_operand2(unsigned char *Asm, int w, int l, f
 }
 
 // step 2 result: lane (w, l) = (row, c = l), columns re d | im d -> out[c + 32 d]
-__device__ __forceinline__ void sp_store(const SplitArgs &a, uint32_t lane_base, long row, int l, float f) {
+// With output rows on 16-byte boundaries the rows are staged in the A
+// operand's space (free once step 2's MMAs completed) and written by one bulk
+// copy each, issued by thread 0, which waits until the copies have read the
+// stage (the CTA's shared memory outlives them).
+__device__ __forceinline__ void sp_store(const SplitArgs &a, uint32_t lane_base, long row, int l, float f,
+                                         unsigned char *Asm, int tid) {
     float yr[32], yi[32];
     tmem_ld32(lane_base + 0, yr);
     tmem_ld32(lane_base + 32, yi);
     tc::tmem_ld_wait();
+    if (a.bulk_out) {
+        const int w = tid >> 5;
+        float2 *stg = reinterpret_cast<float2 *>(Asm) + w * SPN;
+#pragma unroll
+        for (int d = 0; d < 32; d++) {
+            float2 o = make_float2(yr[d] * f, yi[d] * f);
+            if (a.inv) o.y = -o.y;
+            stg[l + 32 * d] = o;
+        }
+        tc::fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            const long row0 = row - w;
+            const int nr = (int)min(4L, a.nvec - row0);
+            for (int r = 0; r < nr; r++)
+                tc::bulk_store(a.out + a.off_out + (row0 + r) * a.vs_out, Asm + r * SPN * 8, SPN * 8);
+            tc::bulk_commit();
+            tc::bulk_wait_read();
+        }
+        return;
+    }
     if (row < a.nvec) {
         float2 *dst = a.out + a.off_out + row * a.vs_out;
 #pragma unroll
@@ -259,7 +286,7 @@ __device__ __forceinline__ bool sp_group(const SplitArgs &a, unsigned char *Asm,
     *pending = ok ? 2u : 1u;
     tc::fence_after_sync();
     if (!ok) return false;
-    sp_store(a, lane_base, row, l, (a.has_scale ? a.scale : 1.f) / (s1 * s2));
+    sp_store(a, lane_base, row, l, (a.has_scale ? a.scale : 1.f) / (s1 * s2), Asm, tid);
     // the accumulator is read out before the next group's step 1 writes it
     tc::fence_before_sync();
     return true;
@@ -432,6 +459,7 @@ bool launch_split_f32(const Job &j, cudaStream_t st) {
     // chunks end at byte 16 * SP_B_LBO - 1 of B: both inside their operands
     const long ngroups = (j.nvec + 3) / 4;
     a.bulk_rows = ((uintptr_t)ci.re % 16) == 0 && (ci.off % 2) == 0 && (j.nvec == 1 || (ci.vs % 2) == 0);
+    a.bulk_out = ((uintptr_t)co.re % 16) == 0 && (co.off % 2) == 0 && (j.nvec == 1 || (co.vs % 2) == 0);
     const size_t smem = SP_A_BYTES + SP_B_BYTES;
     static bool attr[2] = {false, false};
     if (!attr[bf]) {

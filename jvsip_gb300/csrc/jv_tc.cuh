@@ -120,6 +120,16 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t b
                  :: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(mbar)) : "memory");
 }
 
+// 1-D bulk copy from shared to global memory in this thread's bulk group
+// (16-byte aligned addresses, a multiple of 16 bytes); commit, and wait until
+// the committed copies have read their shared-memory sources
+__device__ __forceinline__ void bulk_store(void *gdst, const void *ssrc, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                 :: "l"(gdst), "r"(smem_addr(ssrc)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+
 // 32 lanes x 32 bits, 16 consecutive columns per thread
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     uint32_t r[16];

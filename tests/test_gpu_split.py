@@ -126,3 +126,23 @@ def test_split_form_unaligned_rows():
     # the gaps between rows keep their (zero) values
     for r in range(Mr - 1):
         assert c[off + r * pitch + N] == 0
+
+
+@pytest.mark.parametrize("in_off,out_off", [(0, 1), (1, 0)], ids=["out-odd", "in-odd"])
+def test_split_form_mixed_alignment(in_off, out_off):
+    # one side on 16-byte row boundaries (bulk copies), the other 8 bytes off
+    Mr = 21
+    z = scaled_rows(Mr, 47)
+    x = np.zeros(2 * (in_off + Mr * N), np.float32)
+    c = z.reshape(-1)
+    x[2 * in_off::2], x[2 * in_off + 1::2] = c.real, c.imag
+    y = np.full(2 * (out_off + Mr * N), 9.0, np.float32)
+    bx, by = J.CBlock(x, admit=True), J.CBlock(y, admit=True)
+    p = J.FFTM(J.KIND_CCOP, Mr, N, 1.0, -1, J.VSIP_ROW)
+    p.setform(J.JVSIP_FORM_SPLIT_BF16)
+    p.ccfftmop(bx.view(in_off, N, Mr, 1, N), by.view(out_off, N, Mr, 1, N))
+    assert J.lib().jvsip_gpu_synchronize() == 0, J.last_error()
+    by.release(True)
+    got = (y[2 * out_off::2] + 1j * y[2 * out_off + 1::2].astype(np.float64)).reshape(Mr, N)
+    assert rows_worst(got, np.fft.fft(z, axis=1)) <= 1e-5
+    assert np.all(y[:2 * out_off] == 9.0)
