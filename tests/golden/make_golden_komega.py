@@ -39,6 +39,7 @@ CASES = [
     ("kw_96x1536_rowfreq", 96, 1536, 1540, 4, "row", "col", 5, 0.5, 5),
     ("kw_12x250", 12, 250, 250, 0, "col", "row", 0, 1.0, 6),
     ("kw_60x2048", 60, 2048, 2048, 0, "row", "row", 0, 0.0625, 7),
+    ("kw_64x256_rowfreq", 64, 256, 258, 2, "row", "row", 1, 0.2, 8),
 ]
 
 
