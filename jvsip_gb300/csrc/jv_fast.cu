@@ -1,17 +1,11 @@
-// jv_fast.cu -- register-resident kernels (single precision, interleaved or
-// split complex) for rows of unit element stride and any pitch, and for
-// column tiles (adjacent transforms of any element stride).
-//
-// A transform of N = R1*R2*...*Rp points is held by T threads, E = N/T
-// complex values each, in registers.  Pass 1 reads global memory directly
-// (element t + T*b + r*N/R1: consecutive threads read consecutive elements),
-// the middle passes exchange through shared memory, and the last pass writes
-// global memory directly (element t + T*b + r*N/Rp, again coalesced): the
-// self-sorting Stockham order needs no digit-reversal pass, so every point is
-// read from and written to HBM exactly once.  Shared memory is indexed
-// i + (i >> 4) (power-of-two passes conflict-free for 8-byte elements) with
-// row pitches chosen per tile shape (fast_pitch).  Several transforms share a
-// CTA when N is small.
+// jv_fast.cu -- launchers of the register-resident kernel (jv_fast.cuh) for
+// single-precision c2c calls: rows of unit element stride and any pitch,
+// column tiles (adjacent transforms of any element stride), interleaved or
+// split complex; the steps and Stockham passes of long transforms; the
+// k-omega power transforms; and the radix schedule each length uses
+// (fast_radices), from which the plans build the kernel's per-pass twiddle
+// tables.  Each case names the CTA shape (T threads per transform, RPC
+// transforms per CTA) that measured fastest.
 #include <stdio.h>
 #include <stdlib.h>
 
