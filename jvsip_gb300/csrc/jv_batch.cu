@@ -355,7 +355,7 @@ static bool upload(const BatchBuild &bb, DevBatch &db) {
 template <int CBT>
 static bool launch_class(const DevBatch &db, int c, cudaStream_t st) {
     Device *d = device();
-    static bool attr = false;
+    static std::atomic<bool> attr{false};  // set once; concurrent first calls both set it
     if (!attr) {
         if (!cuda_ok(cudaFuncSetAttribute(k_batch<CBT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)d->smem_optin - 512),
@@ -370,7 +370,7 @@ static bool launch_class(const DevBatch &db, int c, cudaStream_t st) {
 
 static bool launch_cols(const DevBatch &db, cudaStream_t st) {
     Device *d = device();
-    static bool attr = false;
+    static std::atomic<bool> attr{false};  // set once; concurrent first calls both set it
     if (!attr) {
         if (!cuda_ok(cudaFuncSetAttribute(k_batch_cols, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)d->smem_optin - 512),

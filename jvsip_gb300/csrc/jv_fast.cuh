@@ -412,7 +412,7 @@ static bool launch_fast_n(const Job &j, cudaStream_t st) {
     if ((FXK & FX_POWER) != 0 && !a.gram) return false;
     constexpr int NP = fast_pitch<N, RPC, COLS>();
     size_t smem = (size_t)RPC * NP * sizeof(float2);
-    static bool attr = false;
+    static std::atomic<bool> attr{false};  // set once; concurrent first calls both set it
     if (!attr) {
         if (smem > 48 * 1024 &&
             !cuda_ok(cudaFuncSetAttribute(k_fast<N, T, RPC, L, SPLIT, COLS, TW, SP, RM, FXK>,

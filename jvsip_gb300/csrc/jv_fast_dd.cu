@@ -177,7 +177,7 @@ static bool launch_dd_n(const Job &j, cudaStream_t st) {
     if (!a.tw) return false;
     constexpr int NP = N + N / 16;
     const size_t smem = (size_t)RPC * NP * sizeof(cdd);
-    static bool attr = false;
+    static std::atomic<bool> attr{false};  // set once; concurrent first calls both set it
     if (!attr) {
         if (smem > 48 * 1024 &&
             !cuda_ok(cudaFuncSetAttribute(k_fast_dd<N, T, RPC, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -208,7 +208,7 @@ static bool launch_smem_v(SmemArgs<T> &a, const Job &j, long vpb, long ld, cudaS
         a.wout = walk_const(a.vec_fast ? vpb : Lout, nthr);
     }
     size_t smem = (size_t)vpb * ld * sizeof(C);
-    static bool attr_set = false;
+    static std::atomic<bool> attr_set{false};  // set once; concurrent first calls both set it
     if (!attr_set) {
         if (!cuda_ok(cudaFuncSetAttribute(k_smem<T, KIND, EMAX, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)(d->smem_optin - kStaticSmem)),

@@ -461,7 +461,7 @@ bool launch_split_f32(const Job &j, cudaStream_t st) {
     a.bulk_rows = ((uintptr_t)ci.re % 16) == 0 && (ci.off % 2) == 0 && (j.nvec == 1 || (ci.vs % 2) == 0);
     a.bulk_out = ((uintptr_t)co.re % 16) == 0 && (co.off % 2) == 0 && (j.nvec == 1 || (co.vs % 2) == 0);
     const size_t smem = SP_A_BYTES + SP_B_BYTES;
-    static bool attr[2] = {false, false};
+    static std::atomic<bool> attr[2]{};  // set once per form; concurrent first calls both set it
     if (!attr[bf]) {
         cudaError_t e = bf ? cudaFuncSetAttribute(k_split1024<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
                            : cudaFuncSetAttribute(k_split1024<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
