@@ -1025,7 +1025,7 @@ void vsip_crfftop_d(const vsip_fft_d *p, const vsip_cvview_d *z, const vsip_vvie
 }
 
 const char *jvsip_gpu_build_info(void) {
-    static char buf[256];
+    static thread_local char buf[256];  // valid until the calling thread's next call
     Device *d = device();
     snprintf(buf, sizeof(buf), "jvsip_gb300 fftm: sm_103a kernels; device %d, %d SMs, %zu B smem/block",
              d ? d->id : -1, d ? d->sms : 0, d ? d->smem_optin : (size_t)0);

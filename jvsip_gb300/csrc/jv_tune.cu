@@ -7,9 +7,12 @@
 // live in memory and in a versioned text cache, one line per key, keyed also
 // by the GPU name, in $JVSIP_GPU_TUNE_CACHE or ~/.cache/jvsip_gb300/tune-v2.txt
 // (safe to delete).  Lengths that were never tuned use the heuristic below.
+#include <errno.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <sys/stat.h>
+#include <sys/types.h>
 
 #include <map>
 #include <mutex>
@@ -53,11 +56,23 @@ static void load_cache() {
     fclose(f);
 }
 
+// every directory of `dir` that does not exist yet, created in turn (mode
+// 0755); true when the whole path exists as a directory afterwards
+static bool make_dirs(const std::string &dir) {
+    if (dir.empty()) return true;
+    for (size_t i = 1; i <= dir.size(); i++) {
+        if (i < dir.size() && dir[i] != '/') continue;
+        const std::string part = dir.substr(0, i);
+        if (mkdir(part.c_str(), 0755) != 0 && errno != EEXIST) return false;
+    }
+    struct stat st;
+    return stat(dir.c_str(), &st) == 0 && S_ISDIR(st.st_mode);
+}
+
 static void save_entry(long N, int prec, int vf, long per) {
     std::string p = cache_path();
-    std::string dir = p.substr(0, p.find_last_of('/'));
-    std::string mk = "mkdir -p '" + dir + "' 2>/dev/null";
-    if (system(mk.c_str()) != 0) return;
+    const size_t slash = p.find_last_of('/');
+    if (slash != std::string::npos && !make_dirs(p.substr(0, slash))) return;
     FILE *f = fopen(p.c_str(), "a");
     if (!f) return;
     fprintf(f, "%s %ld %d %d %ld\n", g_gpu.empty() ? "gpu" : g_gpu.c_str(), N, prec, vf, per);
