@@ -130,7 +130,8 @@ bool launch_fast_sp_f32(const Job &j, cudaStream_t st) {
 // transforms (a column-major spectrum, as kw.c creates it) on the row
 // mapping, adjacent transforms (a row-major one) as column tiles.
 bool launch_fast_komega_power_f32(const Job &j, cudaStream_t st) {
-    if (j.prec != P_F32 || j.kind != K_C2C || !j.gram || !j.twp || j.lp || j.nbatch > 1 || j.tw_lo) return false;
+    if (j.no_fast || j.prec != P_F32 || j.kind != K_C2C || !j.gram || !j.twp || j.lp || j.nbatch > 1 || j.tw_lo)
+        return false;
     const CView &ci = j.cin, &co = j.cout;
     if (ci.cst != 2 || co.cst != 2 || (const float *)ci.im != (const float *)ci.re + 1 ||
         (const float *)co.im != (const float *)co.re + 1 || ((uintptr_t)ci.re % 8) || ((uintptr_t)co.re % 8))

@@ -68,7 +68,8 @@ bool launch_fast_real_f32(const Job &j, cudaStream_t st) {
 // The k-omega pipeline's R2C rows: tapers applied to the loaded real pairs
 // and written back (kw.c's two vsip_vmmul_f) in the first pass.
 bool launch_fast_komega_r2c_f32(const Job &j, cudaStream_t st) {
-    if (j.prec != P_F32 || j.kind != K_R2C || !j.thalf || !j.twp || !j.taper_n || !j.taper_t || !j.taper_back)
+    if (j.no_fast || j.prec != P_F32 || j.kind != K_R2C || !j.thalf || !j.twp || !j.taper_n || !j.taper_t ||
+        !j.taper_back)
         return false;
     if (j.nvec <= 0 || j.nvec > 0x7fffffffL) return false;
     if (!real_rows(j.rin, 2 * j.N, j.nvec) || !complex_out(j.cout, j.N + 1, j.nvec)) return false;

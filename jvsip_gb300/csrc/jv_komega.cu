@@ -36,7 +36,7 @@ static void plan_job(Job &j, const Plan *p, int kind) {
     j.twg = p->d_twg;
     j.pc = p->d_pc;
     j.form = 0;
-    j.no_fast = true;
+    j.no_fast = p->no_fast;  // JVSIP_GPU_NO_FAST: the shared-memory kernel's instances only
     j.tma_columns = p->tma_columns;
     j.npass = (int)p->radix.size();
     for (int i = 0; i < j.npass && i < 40; i++) j.radix[i] = p->radix[i];
