@@ -440,7 +440,8 @@ int jvsip_komega_f(const vsip_fftm_f *rcfftm, const vsip_fftm_f *ccfftm,
  * memory that is part of the library (held on every GPU that loads it until
  * exit): mN*MN may not exceed 1048576 complex points, larger calls return an
  * error.  The array's address is looked up on the first call on each device,
- * so make that call before any stream capture.  All calls share the array and
+ * so make that call before any stream capture.  x and y must be the same buffer
+ * or not overlap.  All calls share the array and
  * it keeps the last call's contents; calls that overlap on the GPU race on it.
  * Work is queued on the library stream (jvsip_gpu_stream); returns 0 when it
  * was queued. */

@@ -261,6 +261,11 @@ constexpr int pass_k(int EMAX, int R) { return R <= 8 ? (EMAX + R - 1) / R : (EM
 // Radix codelets of the general kernel, in the order of its pass loops.
 constexpr int kRadices = 13;
 constexpr int kRadixList[kRadices] = {16, 15, 14, 12, 10, 9, 8, 7, 6, 5, 4, 3, 2};
+inline bool gpass_codelet_host(int R) {
+    for (int i = 0; i < kRadices; i++)
+        if (kRadixList[i] == R) return true;
+    return false;
+}
 // device pass radices for length N: for 2^a 3^b 5^c 7^d the fewest passes of
 // the codelets above (largest first), else radix 8/4/2, 3, 5, 7, then any other prime
 std::vector<int> pass_radices(long N, bool *smooth, long maxt);  // maxt: threads per CTA of the shared-memory kernel

@@ -1230,36 +1230,66 @@ __device__ __forceinline__ void gpass_body(const GPassArgs<T> &a, long v, int j)
     }
 }
 
+// Radices with a codelet; any other radix is an odd prime taken as a direct sum.
+__host__ __device__ __forceinline__ bool gpass_codelet(int R) {
+    return R == 2 || R == 3 || R == 4 || R == 5 || R == 6 || R == 7 || R == 8 || R == 9 || R == 10 || R == 12 ||
+           R == 14 || R == 15 || R == 16;
+}
+
+// Output k of butterfly j of a prime-radix pass as the direct sum over its R
+// inputs (the O(R^2) DFT of c_VSIP_src/VI_fftm_building_blocks_f.h:95-155,
+// VI_dftm_f, with the inter-pass twiddle folded into the load).  One thread
+// per output keeps the work of a thread at R complex multiply-adds, so a
+// transform of prime length spreads over N threads.
 template <typename T>
-__device__ __forceinline__ void gpass_generic(const GPassArgs<T> &a, long v, int j) {
+__device__ __forceinline__ void gpass_generic(const GPassArgs<T> &a, long v, int j, int k) {
     typedef typename cplx_t<T>::t C;
     const int R = a.R, NR = a.N / R;
-    int m = j % a.Ns;
-    long st = (long)m * (a.N / (a.Ns * R));
-    long base = (long)(j - m) * R + m;
+    const int m = j % a.Ns;
+    const long st = (long)m * (a.N / (a.Ns * R));
+    const long base = (long)(j - m) * R + m;
     const long rstep = a.N / R;  // table index step of exp(-2 pi i/R)
-    for (int k = 0; k < R; k++) {
-        C acc = mk<C>((T)0, (T)0);
-        for (int n = 0; n < R; n++) {
-            C c;
-            if (a.src_real) c = mk<C>(a.rsrc.load(v, 2 * (j + n * NR)), a.rsrc.load(v, 2 * (j + n * NR) + 1));
-            else c = a.src.load(v, j + n * NR);
-            if (a.conj_in) c.y = -c.y;
-            if (m && n) c = cmul(c, __ldg(&a.tw[n * st]));
-            long e = ((long)n * k) % R;
-            C w = __ldg(&a.tw[e * rstep]);
-            acc = cadd(acc, cmul(c, w));
-        }
-        if (a.conj_out) acc.y = -acc.y;
-        if (a.has_scale) acc = cscale(acc, a.scale);
-        a.dst.store(v, base + (long)k * a.Ns, acc);
+    C acc = mk<C>((T)0, (T)0);
+    int e = 0;                   // (n * k) mod R
+    for (int n = 0; n < R; n++) {
+        C c;
+        if (a.src_real) c = mk<C>(a.rsrc.load(v, 2 * (j + n * NR)), a.rsrc.load(v, 2 * (j + n * NR) + 1));
+        else c = a.src.load(v, j + n * NR);
+        if (a.conj_in) c.y = -c.y;
+        if (m && n) c = cmul(c, __ldg(&a.tw[n * st]));
+        C w = __ldg(&a.tw[(long)e * rstep]);
+        acc = cadd(acc, cmul(c, w));
+        e += k;
+        if (e >= R) e -= R;
     }
+    if (a.conj_out) acc.y = -acc.y;
+    if (a.has_scale) acc = cscale(acc, a.scale);
+    a.dst.store(v, base + (long)k * a.Ns, acc);
+}
+
+// Work items of one pass: a butterfly (j) for codelet radices, an output
+// (j, k) of a butterfly for direct-sum radices.
+__host__ __device__ __forceinline__ long gpass_items(long nvec, int N, int R) {
+    return gpass_codelet(R) ? nvec * (N / R) : nvec * (long)N;
 }
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_gpass(const GPassArgs<T> pa) {
     const GPassArgs<T> a = pa;
     const long NR = a.N / a.R;
+    if (!gpass_codelet(a.R)) {
+        // consecutive threads take consecutive butterflies j of one output k,
+        // so their loads of input n are adjacent
+        const long total = a.nvec * (long)a.N;
+        for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+            long v = i / a.N;
+            long rem = i - v * a.N;
+            int k = (int)(rem / NR);
+            int j = (int)(rem - (long)k * NR);
+            gpass_generic<T>(a, v, j, k);
+        }
+        return;
+    }
     const long total = a.nvec * NR;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
         long v = i / NR;
@@ -1277,8 +1307,7 @@ __global__ void __launch_bounds__(256) k_gpass(const GPassArgs<T> pa) {
             case 12: gpass_body<T, 12>(a, v, j); break;
             case 14: gpass_body<T, 14>(a, v, j); break;
             case 15: gpass_body<T, 15>(a, v, j); break;
-            case 16: gpass_body<T, 16>(a, v, j); break;
-            default: gpass_generic<T>(a, v, j); break;
+            default: gpass_body<T, 16>(a, v, j); break;
         }
     }
 }

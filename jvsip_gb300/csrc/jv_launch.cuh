@@ -375,7 +375,7 @@ static CView dense_view(void *buf, long N) {
 template <typename T>
 static bool gpass(const GPassArgs<T> &a, cudaStream_t st) {
     Device *d = device();
-    long total = a.nvec * (a.N / a.R);
+    long total = gpass_items(a.nvec, a.N, a.R);
     long grid = (total + 255) / 256;
     long gmax = (long)d->sms * 32;
     if (grid > gmax) grid = gmax;

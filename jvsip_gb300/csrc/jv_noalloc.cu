@@ -16,9 +16,10 @@
 // beforehand (plan creation allocates; this call does not).  The array holds
 // at most JV_NOALLOC_MAX complex points per buffer, so mN * MN of the plan must
 // not exceed it; larger calls are rejected with an error.  The array lives on
-// every GPU that loads the library until the process exits.  Its address is
-// looked up once per device, on the first call made with that device current;
-// make that first call before any stream capture begins.  Every call uses the
+// every GPU that loads the library until the process exits.  Its address on
+// the library's device is looked up once, by the first call (which makes that
+// device current for the lookup); make that first call before any stream
+// capture begins.  Every call uses the
 // same array and it keeps the last call's contents; nothing in it has to start
 // at zero because every pass writes all the scratch it later reads.  Calls are
 // issued on the library's stream, so calls from this library are ordered;
@@ -36,27 +37,26 @@ constexpr long JV_NOALLOC_MAX = 1L << 20;   // complex points per scratch buffer
 static __device__ __align__(256) float2 g_noalloc_scratch[2 * JV_NOALLOC_MAX];
 
 static std::mutex g_na_mu;
-static float2 *g_na_addr[64];
+static float2 *g_na_addr = nullptr;  // device address of the array on the library's device
 
-// Device address of the scratch array on the current device (looked up once).
-static float2 *noalloc_scratch() {
-    int dev = -1;
-    if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return nullptr;
-    if (dev < 0 || dev >= 64) {
-        set_error(E_UNSUPPORTED, "device index out of range for the fixed scratch table");
+// Device address of the scratch array on the library's device, looked up on
+// the first call with that device made current for the lookup (the library
+// runs all its work on one device, Device::id, and its stream).
+static float2 *noalloc_scratch(const Device *d) {
+    std::lock_guard<std::mutex> lk(g_na_mu);
+    if (g_na_addr) return g_na_addr;
+    int cur = -1;
+    if (!cuda_ok(cudaGetDevice(&cur), "cudaGetDevice")) return nullptr;
+    if (cur != d->id && !cuda_ok(cudaSetDevice(d->id), "cudaSetDevice to the library's device")) return nullptr;
+    void *ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (cur != d->id) cudaSetDevice(cur);
+    if (e != cudaSuccess || !ptr) {
+        set_error(E_CUDA, std::string("cudaGetSymbolAddress of the fixed scratch: ") + cudaGetErrorString(e));
         return nullptr;
     }
-    std::lock_guard<std::mutex> lk(g_na_mu);
-    if (!g_na_addr[dev]) {
-        void *ptr = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-        if (e != cudaSuccess || !ptr) {
-            set_error(E_CUDA, std::string("cudaGetSymbolAddress of the fixed scratch: ") + cudaGetErrorString(e));
-            return nullptr;
-        }
-        g_na_addr[dev] = (float2 *)ptr;
-    }
-    return g_na_addr[dev];
+    g_na_addr = (float2 *)ptr;
+    return g_na_addr;
 }
 
 }  // namespace jv
@@ -78,8 +78,22 @@ extern "C" int jvsip_ccfftm_noalloc_f(const vsip_fftm_f *plan, const void *x, lo
     // consecutive points of a transform (COL plans), in complex elements
     const long need = (p->major == 0) ? N : nv;
     if (x_pitch < need || y_pitch < need) {
-        set_error(E_ARG, "jvsip_ccfftm_noalloc_f: row pitch smaller than the row");
+        set_error(E_ARG, p->major == 0 ? "jvsip_ccfftm_noalloc_f: row pitch smaller than the row (VSIP_ROW plan)"
+                                       : "jvsip_ccfftm_noalloc_f: column pitch smaller than the number of columns "
+                                         "(VSIP_COL plan)");
         return E_ARG;
+    }
+    {
+        // the passes read x while writing y: the two may be one buffer
+        // (in place) but must not overlap otherwise
+        const uintptr_t xb = (uintptr_t)x, yb = (uintptr_t)y;
+        const long span_x = (p->major == 0 ? (nv - 1) * x_pitch + N : (N - 1) * x_pitch + nv);
+        const long span_y = (p->major == 0 ? (nv - 1) * y_pitch + N : (N - 1) * y_pitch + nv);
+        const uintptr_t xe = xb + (uintptr_t)span_x * 8, ye = yb + (uintptr_t)span_y * 8;
+        if (xb != yb && N > 0 && nv > 0 && xb < ye && yb < xe) {
+            set_error(E_ARG, "jvsip_ccfftm_noalloc_f: input and output overlap without being the same buffer");
+            return E_ARG;
+        }
     }
     if (N * nv > JV_NOALLOC_MAX) {
         set_error(E_ARG, "jvsip_ccfftm_noalloc_f: mN*MN exceeds the fixed scratch of 1048576 complex points");
@@ -87,7 +101,7 @@ extern "C" int jvsip_ccfftm_noalloc_f(const vsip_fftm_f *plan, const void *x, lo
     }
     Device *d = device();
     if (!d) return E_NODEVICE;
-    float2 *sc = noalloc_scratch();
+    float2 *sc = noalloc_scratch(d);
     if (!sc) return jvsip_gpu_last_error();
     if (N <= 0 || nv <= 0) return 0;
 

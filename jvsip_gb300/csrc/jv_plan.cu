@@ -11,6 +11,7 @@
 // the device twiddle tables (generated in FP64, rounded to the plan's type)
 // and, for real transforms, the half-angle table exp(-+ i pi k/MN).
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -498,13 +499,39 @@ Plan *plan_of_v(const void *vp) {
     return (p && p->single) ? p : nullptr;
 }
 
+// Radices above 7 that are not codelets are primes taken as a direct sum of
+// R multiply-adds per output point.  A plan whose direct sums would keep the
+// GPU busy for seconds per call (a long prime length, the reference's
+// O(L^2) VI_dftm_f case, c_VSIP_src/VI_fftm_building_blocks_f.h:95-155) is
+// refused at creation: at most 2^38 complex multiply-adds per call in single
+// precision and 2^35 in double (FP64 runs at a small fraction of FP32 here).
+constexpr double kDirectSumMaxF = 274877906944.0;  // 2^38
+constexpr double kDirectSumMaxD = 34359738368.0;   // 2^35
+
+static bool direct_sum_ok(const Plan *p) {
+    double per_point = 0;
+    for (int R : p->radix)
+        if (R > 7 && !gpass_codelet_host(R)) per_point += (double)R;
+    const double work = per_point * (double)p->MN * (double)p->mN;
+    const double lim = p->prec == P_F32 ? kDirectSumMaxF : kDirectSumMaxD;
+    if (work > lim) {
+        char msg[256];
+        snprintf(msg, sizeof msg,
+                 "plan refused: lengths with large prime factors are direct sums; this plan needs %.3g complex "
+                 "multiply-adds per call, above the limit %.3g (%s)",
+                 work, lim, p->prec == P_F32 ? "single precision" : "double precision");
+        set_error(E_UNSUPPORTED, msg);
+        return false;
+    }
+    return true;
+}
+
 // The device plan of M x N transforms (a single FFT is M = 1, VSIP_ROW);
 // *ns and *dft receive the reference's factor count and DFT flag.  Returns
 // nullptr (error recorded, nothing left allocated) on failure.
 template <typename T>
 static Plan *new_plan(int type, vsip_length M, vsip_length N, double scale, int dir, vsip_major major,
                       unsigned ntimes, vsip_alg_hint hint, unsigned long *ns_out, int *dft_out) {
-    if (!device()) return nullptr;
     Plan *p = new (std::nothrow) Plan();
     if (!p) {
         set_error(E_ALLOC, "plan allocation");
@@ -534,6 +561,14 @@ static Plan *new_plan(int type, vsip_length M, vsip_length N, double scale, int 
     p->ntimes = ntimes;
     p->hint = (int)hint;
     p->radix = pass_radices(p->MN, &p->smooth, p->prec == P_F32 ? 1024 : 512);
+    if (!direct_sum_ok(p)) {
+        delete p;
+        return nullptr;
+    }
+    if (!device()) {
+        delete p;
+        return nullptr;
+    }
     unsigned long pn[8], p0[8], pF[8];
     unsigned long ns = ref_factor((unsigned long)p->MN, pn, p0, pF);
     if (ns > 0) {
@@ -562,7 +597,6 @@ static Plan *new_plan(int type, vsip_length M, vsip_length N, double scale, int 
 template <typename VP, typename T>
 static VP *create(int type, vsip_length M, vsip_length N, double scale, int dir, vsip_major major,
                   unsigned ntimes, vsip_alg_hint hint) {
-    if (!device()) return NULL;
     VP *vp = (VP *)calloc(1, sizeof(VP));
     if (!vp) {
         set_error(E_ALLOC, "plan allocation");
@@ -598,7 +632,6 @@ static VP *create(int type, vsip_length M, vsip_length N, double scale, int dir,
 // VI_crfftop_create_f_def.h:32); the reference's work arrays are not needed.
 template <typename FP, typename T>
 static FP *create_v(int type, vsip_length N, double scale, int dir, unsigned ntimes, vsip_alg_hint hint) {
-    if (!device()) return NULL;
     FP *fp = (FP *)calloc(1, sizeof(FP));
     if (!fp) {
         set_error(E_ALLOC, "plan allocation");

@@ -21,15 +21,19 @@ from pyoracle import CCIP, CCOP, CROP, RCOP, CView, RView, sfx  # noqa: F401
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 LIB_PATH = os.path.join(HERE, "_ref", "libvsip_ref.so")
-REF_SRC = os.environ.get("JVSIP_REFERENCE", "/root/reference")
+# the reference checkout (its c_VSIP_src/ is compiled); named only by this variable
+REF_SRC = os.environ.get("JVSIP_REFERENCE", "")
 
 
 def available() -> bool:
-    return os.path.exists(LIB_PATH) or os.path.isdir(os.path.join(REF_SRC, "c_VSIP_src"))
+    return os.path.exists(LIB_PATH) or (bool(REF_SRC) and os.path.isdir(os.path.join(REF_SRC, "c_VSIP_src")))
 
 
 def build() -> str:
     if not os.path.exists(LIB_PATH):
+        if not REF_SRC:
+            raise RuntimeError("oracle/_ref/libvsip_ref.so is not built: set JVSIP_REFERENCE to the jvsip "
+                               "reference checkout (the directory holding c_VSIP_src/)")
         subprocess.check_call(["make", "-f", os.path.join(HERE, "Makefile.ref"), "-j8",
                                "REF=" + REF_SRC], cwd=REPO)
     return LIB_PATH

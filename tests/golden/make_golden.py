@@ -1,9 +1,9 @@
 """Generate the golden fixtures under tests/golden/ from the jvsip reference.
 
-Run in a container that holds the reference sources (default
-/root/reference, override with JVSIP_REFERENCE):
+Run where the reference sources are, with JVSIP_REFERENCE naming the
+reference checkout (the directory holding c_VSIP_src/ and c_VSIP_testing/):
 
-    python tests/golden/make_golden.py
+    JVSIP_REFERENCE=<checkout> python tests/golden/make_golden.py
 
 It writes
   ref_testcases.json  -- the reference's own fftm known-answer tests, parsed
@@ -39,7 +39,9 @@ sys.path.insert(0, os.path.join(REPO, "oracle"))
 import pyoracle as O  # noqa: E402
 import pyref as R  # noqa: E402
 
-REF = os.environ.get("JVSIP_REFERENCE", "/root/reference")
+REF = os.environ.get("JVSIP_REFERENCE", "")
+if not REF or not os.path.isdir(REF):
+    sys.exit("set JVSIP_REFERENCE to the jvsip reference checkout (the directory holding c_VSIP_src/)")
 # outputs up to this size are stored whole; larger ones as a hash plus a sample
 FULL_OUTPUT_BYTES = 40 * 1024
 

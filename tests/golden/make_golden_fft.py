@@ -1,10 +1,10 @@
 """Generate the single-FFT golden fixtures under tests/golden/ from the jvsip
 reference's vector FFT (vsip_ccfftop / ccfftip / rcfftop / crfftop).
 
-Run in a container that holds the reference sources (default
-/root/reference, override with JVSIP_REFERENCE):
+Run where the reference sources are, with JVSIP_REFERENCE naming the
+reference checkout (the directory holding c_VSIP_src/ and c_VSIP_testing/):
 
-    python tests/golden/make_golden_fft.py
+    JVSIP_REFERENCE=<checkout> python tests/golden/make_golden_fft.py
 
 It writes
   fft_kat.json        -- the reference's own single-FFT known-answer tests

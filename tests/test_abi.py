@@ -97,6 +97,21 @@ def test_no_gpu_create_returns_null_with_error():
     assert L.vsip_fft_destroy_d(None) == 0
 
 
+def test_plan_of_a_long_prime_length_is_refused_before_any_device_work():
+    # 1024 rows of the prime length 1048573 are direct sums of about 1.1e12
+    # complex multiply-adds per call; plan creation refuses them (on any host)
+    L = J.lib()
+    L.jvsip_gpu_clear_error()
+    assert L.vsip_ccfftmop_create_f(1024, 1048573, 1.0, -1, 0, 0, 0) is None
+    code, msg = J.last_error()
+    assert "refused" in msg and "multiply-adds" in msg, msg
+    L.jvsip_gpu_clear_error()
+    assert L.vsip_ccfftop_create_d(1048573, 1.0, -1, 0, 0) is None
+    code, msg = J.last_error()
+    assert "refused" in msg, msg
+    L.jvsip_gpu_clear_error()
+
+
 def test_block_lifecycle_without_gpu():
     import numpy as np
     L = J.lib()

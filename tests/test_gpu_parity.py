@@ -3,6 +3,8 @@ host-staged mode (blocks not admitted) and the device-resident mode (blocks
 admitted to device mirrors), against the reference's outputs within
 rel-L2 <= 1e-6*log2(N) (_f) / 1e-14*log2(N) (_d); elements outside the output
 view must be left untouched; and the reference's own known-answer tests."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -59,6 +61,46 @@ def test_plan_attributes_and_schedule():
     assert a.place == 0 and a.dir == 1 and a.major == 1 and abs(a.scale - 0.5) < 1e-7
     assert int(np.prod(q.passes())) == 1000
     assert q.jofk(1000) == O.jofk(1000)
+
+
+class _ViewXX(C.Structure):
+    _fields_ = [("block", C.c_void_p), ("offset", C.c_ulong), ("stride", C.c_long), ("length", C.c_ulong),
+                ("markings", C.c_int)]
+
+
+class PlanObjF(C.Structure):
+    """The leading fields of the plan object, c_VSIP_src/vsip_fftmattributes_f.h:8-38."""
+    _fields_ = [("wt", C.c_void_p), ("temp", C.c_void_p), ("index", C.c_void_p), ("pn", C.c_void_p),
+                ("p0", C.c_void_p), ("pF", C.c_void_p), ("x", C.c_void_p), ("xx", _ViewXX),
+                ("x_r", C.c_void_p), ("x_i", C.c_void_p), ("xp_r", C.c_void_p), ("xp_i", C.c_void_p),
+                ("xst", C.c_long), ("yst", C.c_long), ("xpst", C.c_long), ("ypst", C.c_long),
+                ("scale", C.c_float), ("N", C.c_ulong), ("M", C.c_ulong), ("MN", C.c_ulong), ("mN", C.c_ulong),
+                ("major", C.c_int), ("length", C.c_ulong), ("d", C.c_int), ("type", C.c_int), ("dft", C.c_int),
+                ("ntimes", C.c_uint), ("hint", C.c_int), ("stage", C.c_ulong), ("ext_fftm_obj", C.c_void_p)]
+
+
+def _catalogue_lengths():
+    lens = {11, 13, 17, 1009, 768, 1000, 1, 2, 3, 49, 343, 2401, 6000, 13824}
+    for c in G.cases():
+        if c["kind"] in ("rcop", "crop"):
+            lens.add((c["N"] if c["major"] == 0 else c["M"]) // 2)
+        else:
+            lens.add(c["M"] if c["major"] == 1 else c["N"])
+    for c in G.fft_cases():
+        lens.add(c["N"] // 2 if c["kind"] in ("rcop", "crop") else c["N"])
+    return sorted(n for n in lens if n >= 1)
+
+
+@pytest.mark.parametrize("n", _catalogue_lengths())
+def test_factor_and_digit_reversal_match_the_reference(n):
+    # index work: bit-exact against the oracle's VI_nuV / VI_jofk restatement
+    p = J.FFTM(J.KIND_CCOP, 2, n, 1.0, J.VSIP_FFT_FWD, J.VSIP_ROW)
+    obj = PlanObjF.from_address(p.h)
+    assert obj.MN == n and obj.mN == 2
+    f = O.factor(n)
+    assert obj.length == len(f)
+    assert obj.dft == (1 if f and f[0][0] == 1 and f[0][2] == n else 0)
+    assert p.jofk(n) == O.jofk(n)
 
 
 def test_caller_quirk_scale_minus_one():

@@ -65,3 +65,42 @@ def test_noalloc_in_place_and_limit():
     assert "scratch" in msg
     L.jvsip_gpu_clear_error()
     assert L.jvsip_gpu_kernel_launches() == n0
+
+
+def test_noalloc_column_plan_with_padded_rows():
+    # VSIP_COL: the mN = 24 transforms of MN = 640 points run down the columns
+    # of a row-major matrix whose rows are 27 complex elements apart
+    import torch
+    L = J.lib()
+    M, N, P = 640, 24, 27
+    plan = J.FFTM(J.KIND_CCOP, M, N, 1.0, -1, J.VSIP_COL)
+    for seed in (11, 12):
+        x = O.fill(2 * M * P, seed, 1, np.float32)
+        y = np.zeros_like(x)
+        bx, by = J.CBlock(x.copy()), J.CBlock(y)
+        plan.ccfftmop(bx.view(0, P, M, 1, N), by.view(0, P, M, 1, N))
+        want = y.reshape(M, P, 2)[:, :N]
+        xd = torch.from_numpy(x).cuda()
+        yd = torch.full_like(xd, 3.0)
+        rc = L.jvsip_ccfftm_noalloc_f(plan.h, xd.data_ptr(), P, yd.data_ptr(), P)
+        assert rc == 0, J.last_error()
+        assert L.jvsip_gpu_synchronize() == 0
+        got = yd.cpu().numpy().reshape(M, P, 2)
+        assert np.all(got[:, N:] == 3.0), "padding columns were written"
+        err = np.linalg.norm(got[:, :N].astype(np.float64) - want) / np.linalg.norm(want)
+        assert err <= 1e-6 * np.log2(M), f"rel-L2 {err:.3e}"
+
+
+def test_noalloc_refuses_partly_overlapping_buffers():
+    import torch
+    L = J.lib()
+    M, N = 4, 256
+    plan = J.FFTM(J.KIND_CCOP, M, N, 1.0, -1, J.VSIP_ROW)
+    buf = torch.zeros(2 * (M * N + 64), dtype=torch.float32, device="cuda")
+    n0 = L.jvsip_gpu_kernel_launches()
+    rc = L.jvsip_ccfftm_noalloc_f(plan.h, buf.data_ptr(), N, buf.data_ptr() + 8 * 16, N)
+    assert rc != 0
+    code, msg = J.last_error()
+    assert "overlap" in msg
+    L.jvsip_gpu_clear_error()
+    assert L.jvsip_gpu_kernel_launches() == n0
