@@ -165,6 +165,7 @@ def cpu_leg(x, N, rows_total, gpu_out=None, target_s=10.0, threads=None):
     out = {"value": round(rows * N * 16 / t / 1e9, 4), "unit": "GB/s", "cores": threads, "kind": "port",
            "sample": f"{rows} of {rows_total} rows x {N} points in {t:.2f} s (oracle/fftm_oracle.c, the reference "
                      "algorithm restated bit for bit; the reference sources are absent on this host)"}
+    out["one_thread"] = one_thread_rate(X, N, rows_total, min(target_s / 2, 5.0), O)
     if gpu_out is not None:
         outs = gpu_out if isinstance(gpu_out, dict) else {"": gpu_out}
         sample = sorted({0, 1, rows_total // 3, rows_total // 2, rows_total - 1})
@@ -183,6 +184,23 @@ def cpu_leg(x, N, rows_total, gpu_out=None, target_s=10.0, threads=None):
             out["gpu_rel_l2_vs_fp64_oracle" + sfx] = max(errs_d)
             out["gpu_rel_l2_vs_reference_f32" + sfx] = max(errs_f) if errs_f else None
     return out
+
+
+def one_thread_rate(X, N, rows_total, target_s, O):
+    """The reference algorithm on one thread (the reference library is
+    single-threaded): GB/s over a bounded sample of the rows of X[rows, 2N]."""
+    import numpy as np
+    r0 = min(rows_total, 8)
+    t0 = time.perf_counter()
+    O.ccfftm_rows_mt(np.ascontiguousarray(X[:r0]), -1, 1.0, 1)
+    t0 = time.perf_counter() - t0
+    rows = int(min(rows_total, max(r0, r0 * target_s / max(t0, 1e-4))))
+    xs = np.ascontiguousarray(X[:rows])
+    t = time.perf_counter()
+    O.ccfftm_rows_mt(xs, -1, 1.0, 1)
+    t = time.perf_counter() - t
+    return {"value": round(rows * N * 16 / t / 1e9, 4), "unit": "GB/s", "cores": 1, "kind": "port",
+            "sample": f"{rows} of {rows_total} rows x {N} points in {t:.2f} s on one thread"}
 
 
 def reference_arm(a):
@@ -217,7 +235,8 @@ def reference_arm(a):
             "config": {"workload": "vsip_ccfftmop_f 65536x4096 c64 VSIP_ROW forward scale 1",
                        "sample_rows_per_step": rows},
             "cpu_baseline": {"value": round(value, 4), "unit": "GB/s", "cores": threads, "kind": "port",
-                             "sample": f"{rows} of {total_rows} rows per step"},
+                             "sample": f"{rows} of {total_rows} rows per step",
+                             "one_thread": one_thread_rate(x, N, total_rows, 3.0, O)},
             "e2e": {"value": round(value, 4), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -452,12 +471,69 @@ def other_workload(a):
         plan.setform(J.JVSIP_FORM_PLAIN)
         extra["forms"] = forms
         y = outs[""]
+    if not a.no_cpu and w in ("cfg2col", "cfg2rc", "cfg2cr"):
+        host_in = x if w == "cfg2col" else (xr if w == "cfg2rc" else z)
+        host_out = y if w == "cfg2col" else (z if w == "cfg2rc" else xr)
+        extra.update(cfg2_oracle_check(w, host_in, host_out))
     if not a.no_cpu and w in ("cfg1", "cfg4"):
         extra["cpu_baseline"] = cpu_leg(x, N, M, gpu_out=outs, target_s=min(a.cpu_seconds, 3.0))
         extra["rel_l2_vs_fp64_oracle"] = extra["cpu_baseline"]["gpu_rel_l2_vs_fp64_oracle"]
         for name in extra.get("forms", {}):
             extra["forms"][name]["rel_l2_vs_fp64_oracle"] = extra["cpu_baseline"]["gpu_rel_l2_vs_fp64_oracle_" + name]
     print(json.dumps(line_for(a, nbytes / (ms / 1e3) / 1e9, ms, nbytes, dt, launches, extra)), flush=True)
+
+
+def cfg2_oracle_check(w, xin, yout):
+    """Mixed-radix configurations: sampled transforms of the GPU output against
+    the FP64 oracle on the same inputs (rel-L2, worst sample), and the
+    reference algorithm (the f32 oracle) timed over the whole call on one
+    thread."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    f64, f32 = np.float64, np.float32
+    errs = []
+    if w == "cfg2col":   # 4096 columns of 1000 points, row-major 1000 x 4096
+        M, N = 1000, 4096
+        X, Y = xin.reshape(M, N, 2), yout.reshape(M, N, 2)
+        for j in (0, 1, 1234, 2047, N - 1):
+            col = np.ascontiguousarray(X[:, j]).reshape(-1).astype(f64)
+            ref = O.CView(np.zeros(2 * M), 0, M, 1, 1, M)
+            O.Plan(O.CCOP, 1, M, 1.0, O.FWD, O.ROW, f64).ccfftmop(O.CView(col, 0, M, 1, 1, M), ref)
+            got = np.ascontiguousarray(Y[:, j]).reshape(-1).astype(f64)
+            errs.append(float(np.linalg.norm(got - ref.buf) / np.linalg.norm(ref.buf)))
+        t = time.perf_counter()
+        O.Plan(O.CCOP, M, N, 1.0, O.FWD, O.COL, f32).ccfftmop(
+            O.CView(xin.copy(), 0, N, M, 1, N), O.CView(np.zeros_like(xin), 0, N, M, 1, N))
+        t = time.perf_counter() - t
+        nbytes = 16 * M * N
+    else:
+        M, N, H = 4096, 1536, 769
+        rows = (0, 1, 1000, 2048, M - 1)
+        for r in rows:
+            if w == "cfg2rc":
+                xr = xin.reshape(M, N)[r].astype(f64)
+                ref = O.CView(np.zeros(2 * H), 0, H, 1, 1, H)
+                O.Plan(O.RCOP, 1, N, 1.0, O.FWD, O.ROW, f64).rcfftmop(O.RView(xr, 0, N, 1, 1, N), ref)
+                got = yout.reshape(M, 2 * H)[r].astype(f64)
+            else:
+                zr = xin.reshape(M, 2 * H)[r].astype(f64)
+                ref = O.RView(np.zeros(N), 0, N, 1, 1, N)
+                O.Plan(O.CROP, 1, N, 1.0 / N, O.INV, O.ROW, f64).crfftmop(O.CView(zr, 0, H, 1, 1, H), ref)
+                got = yout.reshape(M, N)[r].astype(f64)
+            errs.append(float(np.linalg.norm(got - ref.buf) / np.linalg.norm(ref.buf)))
+        t = time.perf_counter()
+        if w == "cfg2rc":
+            O.Plan(O.RCOP, M, N, 1.0, O.FWD, O.ROW, f32).rcfftmop(
+                O.RView(xin.copy(), 0, N, M, 1, N), O.CView(np.zeros(2 * M * H, f32), 0, H, M, 1, H))
+        else:
+            O.Plan(O.CROP, M, N, 1.0 / N, O.INV, O.ROW, f32).crfftmop(
+                O.CView(xin.copy(), 0, H, M, 1, H), O.RView(np.zeros(M * N, f32), 0, N, M, 1, N))
+        t = time.perf_counter() - t
+        nbytes = M * (4 * N + 8 * H)
+    return {"rel_l2_vs_fp64_oracle": max(errs), "sampled_transforms": len(errs),
+            "cpu_baseline": {"value": round(nbytes / t / 1e9, 4), "unit": "GB/s", "cores": 1, "kind": "port",
+                             "sample": f"the whole call once on one thread in {t:.2f} s (oracle/fftm_oracle.c)"}}
 
 
 def komega_workload(a, torch, J, L, ext):
@@ -639,13 +715,73 @@ def batching_workload(a, torch, J, L, ext):
 
 
 # ---------------------------------------------------------------- default workload
+def cfg3_variants(a, torch, J, L, ext, bx, by, vx, vy, M, N, x_np):
+    """The rest of the large plain batch on the same admitted 65536 x 4096
+    blocks: vsip_ccfftmop_f inverse (scale 1/4096, x -> y) and
+    vsip_ccfftmip_f in place on y, forward and inverse calls alternating (so
+    the data stays bounded).  Each with CUDA-event times on the library stream
+    and a check: sampled inverse rows against the FP64 oracle, the first
+    in-place forward call (applied to the inverse of x) against x itself, and
+    the in-place round trips against the data they started from."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    nbytes = 16 * M * N
+    inv_op = J.FFTM(J.KIND_CCOP, M, N, 1.0 / N, J.VSIP_FFT_INV, J.VSIP_ROW)
+    fwd_ip = J.FFTM(J.KIND_CCIP, M, N, 1.0, J.VSIP_FFT_FWD, J.VSIP_ROW)
+    inv_ip = J.FFTM(J.KIND_CCIP, M, N, 1.0 / N, J.VSIP_FFT_INV, J.VSIP_ROW)
+    steps = max(2, a.steps)
+    out = {"workload": f"{M}x{N} c64 VSIP_ROW, the default line's admitted blocks", "unit": "GB/s"}
+    call_inv = lambda: L.vsip_ccfftmop_f(inv_op.h, vx.h, vy.h)
+    for _ in range(min(3, a.warmup)):
+        call_inv()
+    per = timed_calls(torch, ext, call_inv, steps)
+    J.check("ccfftmop inverse")
+    by.sync()
+    y_np = by.re
+    X, Y = x_np.reshape(M, 2 * N), y_np.reshape(M, 2 * N)
+    errs = []
+    for r in sorted({0, 1, M // 3, M // 2, M - 1}):
+        ref = O.CView(np.zeros(2 * N), 0, N, 1, 1, N)
+        O.Plan(O.CCOP, 1, N, 1.0 / N, O.INV, O.ROW, np.float64).ccfftmop(
+            O.CView(X[r].astype(np.float64), 0, N, 1, 1, N), ref)
+        errs.append(float(np.linalg.norm(Y[r].astype(np.float64) - ref.buf) / np.linalg.norm(ref.buf)))
+    ms = statistics.mean(per)
+    out["ccfftmop_f_inverse"] = {"value": round(nbytes / (ms / 1e3) / 1e9, 2), "ms_per_step": round(ms, 4),
+                                 "scale": 1.0 / N, "rel_l2_vs_fp64_oracle": max(errs), "sampled_rows": len(errs)}
+    y0 = Y[:64].copy()
+    # in place on y: the first forward call gives back x
+    L.vsip_ccfftmip_f(fwd_ip.h, vy.h)
+    J.check("ccfftmip forward")
+    by.sync()
+    e_first = float(np.linalg.norm(Y[:64].astype(np.float64) - X[:64]) / np.linalg.norm(X[:64].astype(np.float64)))
+    L.vsip_ccfftmip_f(inv_ip.h, vy.h)
+    pf, pi = [], []
+    for _ in range(steps):
+        pf += timed_calls(torch, ext, lambda: L.vsip_ccfftmip_f(fwd_ip.h, vy.h), 1)
+        pi += timed_calls(torch, ext, lambda: L.vsip_ccfftmip_f(inv_ip.h, vy.h), 1)
+    J.check("ccfftmip loop")
+    by.sync()
+    e_rt = float(np.linalg.norm(Y[:64].astype(np.float64) - y0) / np.linalg.norm(y0.astype(np.float64)))
+    mf, mi = statistics.mean(pf), statistics.mean(pi)
+    out["ccfftmip_f_forward"] = {"value": round(nbytes / (mf / 1e3) / 1e9, 2), "ms_per_step": round(mf, 4),
+                                 "rel_l2_first_call_vs_input_x": e_first}
+    out["ccfftmip_f_inverse"] = {"value": round(nbytes / (mi / 1e3) / 1e9, 2), "ms_per_step": round(mi, 4),
+                                 "scale": 1.0 / N,
+                                 f"rel_l2_after_{steps + 1}_round_trips": e_rt}
+    for p in (inv_op, fwd_ip, inv_ip):
+        p.destroy()
+    return out
+
+
 def forms_summary(a):
     """The precision form (cfg4: plain against split FP16 / BF16 on 32768x1024,
     rows scaled by 10^U(-3,3)) and the batching form (cfg5: the 2 GB instance
     sequence, one graph replay against a loop of per-plan calls), each measured
     by its own bench.py run on the same GPU, summarised for the default line."""
     out = {}
-    runs = (("cfg4", ["--cpu-seconds", "2"]), ("cfg5", ["--no-cpu"]))
+    runs = (("cfg4", ["--cpu-seconds", "2"]), ("cfg5", ["--no-cpu"]), ("cfg1", ["--cpu-seconds", "2"]),
+            ("cfg2rc", []), ("cfg2cr", []), ("cfg2col", []))
     for wl, extra in runs:
         cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--workload", wl, "--steps", "20", "--warmup", "5"]
         try:
@@ -661,6 +797,15 @@ def forms_summary(a):
                 "plain": {"value": d["value"], "rel_l2_vs_fp64_oracle": d.get("rel_l2_vs_fp64_oracle")},
                 "split_fp16": f.get("split_fp16"), "split_bf16": f.get("split_bf16"),
                 "hbm_frac_plain": d.get("hbm_frac")}
+        elif wl != "cfg5":
+            out[wl] = {"workload": d["config"]["workload"], "value": d["value"], "unit": "GB/s",
+                       "ms_per_step": d["ms_per_step"], "hbm_frac": d.get("hbm_frac"),
+                       "gpu_launches": d.get("gpu_launches"),
+                       "rel_l2_vs_fp64_oracle": d.get("rel_l2_vs_fp64_oracle"),
+                       "cpu_baseline": d.get("cpu_baseline")}
+            if wl == "cfg1" and isinstance(out[wl]["cpu_baseline"], dict):
+                out[wl]["cpu_baseline"] = {k: v for k, v in out[wl]["cpu_baseline"].items()
+                                           if not k.startswith("gpu_rel")}
         else:
             out["batching_form"] = {
                 "workload": d["config"]["workload"], "unit": "GB/s",
@@ -779,6 +924,10 @@ def main():
         for b in (bxe, bye):
             b.destroy()
     clk = clocks.stop()
+    cpu = None if (a.no_cpu or rank != 0) else cpu_leg(x_np, N, M, gpu_out=y_np, target_s=a.cpu_seconds)
+    variants = None
+    if not a.no_forms:
+        variants = cfg3_variants(a, torch, J, L, ext, bx, by, vx, vy, M, N, x_np)
 
     for v in (vx, vy):
         v.destroy()
@@ -809,13 +958,15 @@ def main():
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": traffic,
                      "kernel_ms": round(kern_ms, 4), "algorithmic_bytes_per_launch": nbytes},
-        "cpu_baseline": None if a.no_cpu else cpu_leg(x_np, N, M, gpu_out=y_np, target_s=a.cpu_seconds),
+        "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(launches),
         "clocks": clk,
     }
     if line["cpu_baseline"]:
         line["rel_l2_vs_fp64_oracle"] = line["cpu_baseline"].get("gpu_rel_l2_vs_fp64_oracle")
+    if variants:
+        line["cfg3_variants"] = variants
     if not a.no_forms and world == 1:
         line["forms"] = forms_summary(a)
     print(json.dumps(line), flush=True)
