@@ -662,8 +662,10 @@ def batching_workload(a, torch, J, L, ext):
     run = lambda: L.jvsip_fftm_batch_run_f(bp)
 
     def loop():
-        for i in range(n):
-            L.vsip_ccfftmop_f(P[i], VI[i], VO[i])
+        # the per-plan loop from C (the library's jvsip_fftm_loop_f): one
+        # vsip_ccfftmop_f call per instance, no Python between the calls
+        if L.jvsip_fftm_loop_f(n, P, VI, VO):
+            raise RuntimeError("jvsip_fftm_loop_f: %s" % (J.last_error(),))
 
     for _ in range(a.warmup):
         run()
@@ -706,7 +708,7 @@ def batching_workload(a, torch, J, L, ext):
     extra = {"config": {"workload": desc, "bytes_per_step": nbytes, "instances": n,
                         "l2": "flushed between calls" if flush is not None else "inputs larger than L2"},
              "plain_loop": {"value": round(loop_gbs, 2), "unit": "GB/s", "ms_per_step": round(ms_loop, 4),
-                            "calls_per_step": n},
+                            "calls_per_step": n, "how": "jvsip_fftm_loop_f: vsip_ccfftmop_f per instance from C"},
              "batched_over_loop": round(value / loop_gbs, 2),
              "batch_vs_loop_max_abs_diff_sampled": same, "rel_l2_vs_fp64_numpy_sampled": max(errs),
              "sampled_instances": len(sample),
@@ -957,6 +959,9 @@ def main():
         "hbm_frac": round(value / world / peak, 4),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": traffic,
+                     "traffic_how": "dram__bytes_read.sum + dram__bytes_write.sum of one k_fast launch in steady state "
+                                    "(ncu --cache-control none, 8192 rows, scaled by rows): "
+                                    "profiles/k_fast_c64_4096_rows.md",
                      "kernel_ms": round(kern_ms, 4), "algorithmic_bytes_per_launch": nbytes},
         "cpu_baseline": cpu,
         "e2e": e2e,

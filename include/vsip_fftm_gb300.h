@@ -374,19 +374,55 @@ jvsip_fftm_batchplan_f *jvsip_fftm_batch_create_f(size_t n, const vsip_fftm_f *c
 int  jvsip_fftm_batch_run_f(jvsip_fftm_batchplan_f *batch);
 int  jvsip_fftm_batch_destroy_f(jvsip_fftm_batchplan_f *batch);
 
+/* The loop the batch replaces, run from C (no reference counterpart; the
+ * reference's callers loop over vsip_ccfftmop_f, c_VSIP_src/VI_ccfftmop_f_def.h:20-29):
+ * call i goes through vsip_ccfftmip_f(plans[i], in[i]) for in-place plans or
+ * when out is NULL or out[i] is NULL, else vsip_ccfftmop_f(plans[i], in[i],
+ * out[i]).  Returns 0, or the first call's error code (the remaining calls
+ * are not made). */
+int  jvsip_fftm_loop_f(size_t n, const vsip_fftm_f *const plans[],
+                       const vsip_cmview_f *const in[], const vsip_cmview_f *const out[]);
+
 /* Autotuner of the batching form: for each of the n lengths (2..16384;
  * vf = 1 for column transforms) time the batch kernel with each candidate
  * number of FFTs per tile and keep the fastest, in memory and in a versioned
  * cache file keyed by GPU name ($JVSIP_GPU_TUNE_CACHE, default
- * ~/.cache/jvsip_gb300/tune-v2.txt).  Untuned lengths use a heuristic.
+ * ~/.cache/jvsip_gb300/tune-v3.txt).  Untuned lengths use a heuristic.
  * Returns 0 on success; jvsip_fftm_autotune_entries() counts cached keys. */
 int  jvsip_fftm_autotune_f(size_t n, const unsigned long *lengths, int vf);
+
+/* Autotuner of the plain c2c calls (no reference counterpart; the reference's
+ * radix order is fixed, c_VSIP_src/VI_nuV.h:22-136): for each of the n
+ * single-precision lengths (2..16384 points of 2^a 3^b 5^c 7^d) and the stride
+ * class cls (0: transforms along contiguous rows, as VSIP_ROW plans; 1:
+ * adjacent transforms, as VSIP_COL plans) time the register-resident kernel
+ * and the shared-memory kernel over radix schedules, transforms per CTA and
+ * values per thread (threads per transform), and keep the fastest in the same
+ * cache.  Plans created afterwards with that length, precision and major use
+ * it.  Returns 0 on success. */
+int  jvsip_fftm_autotune_plain_f(size_t n, const unsigned long *lengths, int cls);
+/* The plain-call entry for (N, single precision, cls): residency (0:
+ * register-resident kernel where one exists, 1: shared-memory kernel),
+ * transforms per CTA (0: heuristic), values per thread and pass (0: automatic)
+ * and up to maxr radices of the schedule; any pointer may be NULL.  Returns
+ * the number of passes of the schedule, 0 when the length is untuned. */
+int  jvsip_fftm_autotune_plain_entry_f(unsigned long N, int cls, int *res, int *vpb, int *emax, int *radices,
+                                       int maxr);
 long jvsip_fftm_autotune_entries(void);
 
 /* Library / device information for tools (kernels compiled, SM count). */
 const char *jvsip_gpu_build_info(void);
-/* Device-side synchronisation: returns when all work this library queued has finished. */
+/* Device-side synchronisation: returns when all work this library queued has
+ * finished; E_DEVICE (6) when a kernel's bounded wait expired since the last
+ * synchronisation (the error is also recorded; the context stays usable). */
 int jvsip_gpu_synchronize(void);
+/* Test hook of the bounded device waits (no reference counterpart): while on
+ * is nonzero, launches of the shared-memory kernel's TMA-staged column tiles
+ * wait, after all their boxes have landed, on a barrier phase that nothing
+ * completes, so that the wait runs out (short poll limit, no copy in flight)
+ * and the kernel reports through the status word that the next
+ * jvsip_gpu_synchronize returns as E_DEVICE.  Returns 0. */
+int jvsip_gpu_test_wait_expiry(int on);
 /* The CUDA stream (cudaStream_t, as void*) all of this library's device work
  * is ordered on; callers may record events on it or make their streams wait. */
 void *jvsip_gpu_stream(void);

@@ -62,7 +62,8 @@ EXPORTS = [
     "vsip_cvcreate_f", "vsip_cvcreate_d", "vsip_vcreate_f", "vsip_vcreate_d",
     "vsip_cvdestroy_f", "vsip_cvdestroy_d", "vsip_vdestroy_f", "vsip_vdestroy_d",
     "vsip_cvalldestroy_f", "vsip_cvalldestroy_d", "vsip_valldestroy_f", "vsip_valldestroy_d",
-    "jvsip_komega_f", "jvsip_fftm_setform_d", "jvsip_fftm_getform_d",
+    "jvsip_komega_f", "jvsip_fftm_setform_d", "jvsip_fftm_getform_d", "jvsip_fftm_loop_f",
+    "jvsip_fftm_autotune_plain_f", "jvsip_fftm_autotune_plain_entry_f", "jvsip_gpu_test_wait_expiry",
 ]
 
 
@@ -189,9 +190,13 @@ def lib(load_only: bool = False):
     L.jvsip_gpu_build_info.restype = C.c_char_p
     L.jvsip_gpu_stream.restype = vp
     L.jvsip_gpu_kernel_launches.restype = C.c_ulong
+    L.jvsip_gpu_test_wait_expiry.argtypes = [C.c_int]
     L.jvsip_ccfftm_noalloc_f.argtypes = [vp, vp, C.c_long, vp, C.c_long]
     L.jvsip_fftm_autotune_f.argtypes = [C.c_size_t, vp, C.c_int]
     L.jvsip_fftm_autotune_entries.restype = C.c_long
+    L.jvsip_fftm_autotune_plain_f.argtypes = [C.c_size_t, vp, C.c_int]
+    ip = C.POINTER(C.c_int)
+    L.jvsip_fftm_autotune_plain_entry_f.argtypes = [C.c_ulong, C.c_int, ip, ip, ip, ip, C.c_int]
     L.jvsip_fftm_setform_f.argtypes = [vp, C.c_int]
     L.jvsip_fftm_getform_f.argtypes = [vp]
     L.jvsip_fftm_setform_d.argtypes = [vp, C.c_int]
@@ -201,6 +206,7 @@ def lib(load_only: bool = False):
     L.jvsip_fftm_batch_create_f.argtypes = [C.c_size_t, vp, vp, vp]
     L.jvsip_fftm_batch_run_f.argtypes = [vp]
     L.jvsip_fftm_batch_destroy_f.argtypes = [vp]
+    L.jvsip_fftm_loop_f.argtypes = [C.c_size_t, vp, vp, vp]
     L.jvsip_fftm_passes.argtypes = [vp, C.POINTER(C.c_int), C.c_int]
     L.jvsip_fftm_graphs.argtypes = [vp]
     L.jvsip_fftm_graphs.restype = C.c_int

@@ -1,6 +1,7 @@
 // jv_batch.cu -- batching form: many independent c2c fftm calls (uneven
 // lengths 2^a 3^b 5^c 7^d, uneven row counts, mixed directions and ROW/COL
-// majors) in one persistent launch.
+// majors) in one launch per CTA-size class, fed by a device queue of tile
+// descriptors.
 //
 // The host cuts every call into tiles of transforms (FFTs per tile from the
 // autotuner's cache, or a heuristic), gives each tile the smallest CTA size
@@ -8,9 +9,11 @@
 // descriptor queue per size, largest tiles first.  One launch per size
 // consumes its queue, one descriptor per CTA -- no CTA ever waits on another
 // -- running the general kernel's fused c2c passes on each tile; the launches
-// run side by side on forked streams.  A captured batch
-// (jvsip_fftm_batch_create_f) records the launches in a CUDA graph once;
-// jvsip_fftm_batch_run_f replays it.
+// run side by side on forked streams.  Each CTA first asks L2 for the input
+// of the descriptor one resident wave further down its queue (the CTA that
+// will take this SM slot later), so later tiles' DRAM reads overlap earlier
+// tiles' passes.  A captured batch (jvsip_fftm_batch_create_f) records the
+// launches in a CUDA graph once; jvsip_fftm_batch_run_f replays it.
 //
 // No reference counterpart: VSIPL has no multi-plan call; the reference can
 // only loop plan by plan (c_VSIP_src/VI_ccfftmop_f_def.h:20-29 per call).
@@ -71,6 +74,31 @@ __device__ __forceinline__ void batch_tile(const TileDesc &d, float2 *s) {
     c2c_tile<float, BEMAX>(s, d.ld, d.nt, d.passes, d.twg, d.pc, io);
 }
 
+__device__ __forceinline__ void prefetch_l2_line(const void *p) {
+    asm volatile("{\n\t.reg .u64 a;\n\tcvta.to.global.u64 a, %0;\n\tprefetch.global.L2 [a];\n\t}" :: "l"(p));
+}
+
+// Ask L2 for the input of tile d: one 128-byte line per thread and step.
+// Transforms contiguous in memory (|es| = 1) go by 16-element segments of each
+// transform, adjacent transforms (|vs| = 1) by 16-element segments of each
+// point's row of transforms; other layouts are not prefetched.
+__device__ __forceinline__ void prefetch_tile(const TileDesc &d, int tid, int nthr) {
+    const float2 *base = reinterpret_cast<const float2 *>(d.in) + (d.in_off + d.v0 * d.in_vs);
+    if (d.in_es == 1) {
+        const int L = (d.N + 15) >> 4, tot = L * d.nt;
+        for (int i = tid; i < tot; i += nthr) {
+            const int v = i / L, l = i - v * L;
+            prefetch_l2_line(base + (long)v * d.in_vs + 16 * l);
+        }
+    } else if (d.in_vs == 1) {
+        const int L = (d.nt + 15) >> 4, tot = L * d.N;
+        for (int i = tid; i < tot; i += nthr) {
+            const int n = i / L, l = i - n * L;
+            prefetch_l2_line(base + (long)n * d.in_es + 16 * l);
+        }
+    }
+}
+
 // One launch over the whole queue: CTA b takes descriptor b.  The queue is
 // sorted largest tile first, so the hardware's in-order CTA dispatch hands the
 // long tiles out first and the short ones fill the tail.  (A persistent
@@ -79,14 +107,19 @@ __device__ __forceinline__ void batch_tile(const TileDesc &d, float2 *s) {
 // spills the codelet registers at every block size, so the loop-free form is
 // used.)
 template <int CBT>
-__global__ void __launch_bounds__(CBT, 1024 / CBT) k_batch(const TileDesc *__restrict__ q, int ntiles) {
+__global__ void __launch_bounds__(CBT, 1024 / CBT) k_batch(const TileDesc *__restrict__ q, int ntiles, int ahead) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *s = reinterpret_cast<float2 *>(smem_raw);
-    __shared__ TileDesc sd;  // descriptor fields are re-read from shared memory, not held in registers
+    __shared__ TileDesc sd, sn;  // descriptor fields are re-read from shared memory, not held in registers
     const int t = blockIdx.x;
     if (t >= ntiles) return;
-    if (threadIdx.x == 0) sd = q[t];
+    const int tn = t + ahead;  // the tile that takes this slot a wave later
+    if (threadIdx.x == 0) {
+        sd = q[t];
+        if (ahead > 0 && tn < ntiles) sn = q[tn];
+    }
     __syncthreads();
+    if (ahead > 0 && tn < ntiles) prefetch_tile(sn, threadIdx.x, blockDim.x);
     batch_tile(sd, s);
 }
 
@@ -363,7 +396,14 @@ static bool launch_class(const DevBatch &db, int c, cudaStream_t st) {
             return false;
         attr = true;
     }
-    k_batch<CBT><<<db.n[c], CBT, db.smem[c], st>>>(db.q + db.off[c], db.n[c]);
+    // CTAs resident at once for this class: the descriptor that many places
+    // further down the queue is the one a finishing CTA's slot takes next
+    int per_sm = 0;
+    if (!cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<CBT>, CBT, db.smem[c]),
+                 "batch occupancy"))
+        return false;
+    const int ahead = std::max(1, per_sm) * d->sms;
+    k_batch<CBT><<<db.n[c], CBT, db.smem[c], st>>>(db.q + db.off[c], db.n[c], ahead);
     count_launch();
     return cuda_ok(cudaGetLastError(), "k_batch launch");
 }
@@ -535,6 +575,26 @@ int jvsip_fftm_batch_run_f(jvsip_fftm_batchplan_f *b) {
     for (const void *blk : b->blocks) {
         Mirror *m = mirror_find(blk);
         if (m) m->device_newer = true;
+    }
+    return 0;
+}
+
+int jvsip_fftm_loop_f(size_t n, const vsip_fftm_f *const plans[], const vsip_cmview_f *const in[],
+                      const vsip_cmview_f *const out[]) {
+    if (n && (!plans || !in)) {
+        set_error(E_ARG, "loop: null arrays");
+        return E_ARG;
+    }
+    for (size_t i = 0; i < n; i++) {
+        Plan *p = plan_of(plans[i]);
+        if (!p) {
+            set_error(E_ARG, "loop: not a plan of this library");
+            return E_ARG;
+        }
+        if (p->type == JV_CCFFTIP || !out || !out[i]) vsip_ccfftmip_f(plans[i], in[i]);
+        else vsip_ccfftmop_f(plans[i], in[i], out[i]);
+        const int e = jvsip_gpu_last_error();
+        if (e) return e;
     }
     return 0;
 }

@@ -92,6 +92,11 @@ int *kernel_status() {
     }
     return g_ks;
 }
+// Test hook of the bounded waits (jvsip_gpu_test_wait_expiry).
+static std::atomic<int> g_test_expiry{0};
+bool test_wait_expiry() { return g_test_expiry.load(std::memory_order_relaxed) != 0; }
+void set_test_wait_expiry(int on) { g_test_expiry.store(on ? 1 : 0, std::memory_order_relaxed); }
+
 int kernel_status_check(cudaStream_t st) {
     std::lock_guard<std::mutex> lk(g_ks_mu);
     if (!g_ks) return 0;
@@ -257,6 +262,11 @@ const char *jvsip_gpu_last_error_string(void) { return t_msg.c_str(); }
 void jvsip_gpu_clear_error(void) {
     t_err = 0;
     t_msg.clear();
+}
+
+int jvsip_gpu_test_wait_expiry(int on) {
+    jv::set_test_wait_expiry(on);
+    return 0;
 }
 
 int jvsip_gpu_synchronize(void) {

@@ -110,6 +110,7 @@ struct Job {
     int form = 0;        // JVSIP_FORM_* of the plan
     bool no_fast = false;      // JVSIP_GPU_NO_FAST at plan creation: general kernels only
     bool no_pipeline = false;  // JVSIP_GPU_NO_PIPELINE at plan creation: one staging copy each way
+    int tuned_vpb = 0, tuned_emax = 0;  // the plan's tuned shared-memory kernel shape (0: automatic)
     int tma_columns = -1;      // JVSIP_GPU_TMA_COLUMNS at plan creation: 1 / 0 force TMA-staged
                                // column tiles on / off, -1 (unset) automatic
     // the steps of a long transform (shared-memory kernel, interleaved c2c only)
@@ -205,6 +206,7 @@ bool launch_c2r_unsplit_f64(const Job &j, void *ydst, cudaStream_t s);
 bool launch_c2r_unpack_f32(const Job &j, const void *y, cudaStream_t s);
 bool launch_c2r_unpack_f64(const Job &j, const void *y, cudaStream_t s);
 int *kernel_status();                                 // device word a kernel sets when a bounded wait expired
+bool test_wait_expiry();                              // test hook: TMA-staged tiles make their wait expire
 int kernel_status_check(cudaStream_t s);              // reads and clears it (0 = clean)
 
 // Capacity queries used by the dispatcher.
@@ -224,6 +226,9 @@ struct Plan {
     bool no_fast = false;     // environment switches read once at creation
     bool no_pipeline = false;
     int tma_columns = -1;
+    int tuned_vpb = 0;        // tuned transforms per CTA of the shared-memory kernel (0: heuristic)
+    int tuned_emax = 0;       // tuned complex values per thread and pass, 8 or 16 (0: automatic)
+    bool tuned = false;       // the autotuner's entry for (MN, precision, stride class) was applied
     std::vector<int> radix;   // pass radices of the device kernels (product = MN)
     bool smooth = true;       // every radix is one of the built-in codelets
     void *d_tw = nullptr;     // forward twiddles, MN entries
@@ -261,6 +266,27 @@ constexpr int pass_k(int EMAX, int R) { return R <= 8 ? (EMAX + R - 1) / R : (EM
 // Radix codelets of the general kernel, in the order of its pass loops.
 constexpr int kRadices = 13;
 constexpr int kRadixList[kRadices] = {16, 15, 14, 12, 10, 9, 8, 7, 6, 5, 4, 3, 2};
+// ------------------------------------------------------------------ autotuner
+// A tuned configuration of the c2c path for one (length, precision, stride
+// class): residency (0: the register-resident kernel where an instance exists,
+// 1: the shared-memory kernel), the shared-memory kernel's pass schedule,
+// transforms per CTA (0: heuristic) and complex values a thread keeps per pass
+// (8 or 16; 0: automatic).  Stride class 0: transforms along contiguous rows
+// (VSIP_ROW plans), 1: adjacent transforms (VSIP_COL plans).
+struct PlainTune {
+    int res = 0;
+    std::vector<int> radix;
+    int vpb = 0;
+    int emax = 0;
+};
+bool plain_tuned(long N, int prec, int cls, PlainTune *out);  // the forced or cached entry
+void plain_tune_force(const PlainTune *t);  // this thread's plans use t instead of the cache (nullptr: off)
+// Schedules of the shared-memory kernel for N (2^a 3^b 5^c 7^d): the default
+// (fewest passes, largest radices first) first, then other orders and
+// decompositions with at most one pass more; at most `limit` of them.
+std::vector<std::vector<int>> schedule_candidates(long N, long maxt, size_t limit);
+bool schedule_valid(const std::vector<int> &r, long N, long maxt);
+
 inline bool gpass_codelet_host(int R) {
     for (int i = 0; i < kRadices; i++)
         if (kRadixList[i] == R) return true;

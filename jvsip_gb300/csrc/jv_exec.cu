@@ -661,6 +661,8 @@ static void fill_job(Job &j, const Plan *p, int kind) {
     j.no_fast = p->no_fast;
     j.no_pipeline = p->no_pipeline;
     j.tma_columns = p->tma_columns;
+    j.tuned_vpb = p->tuned_vpb;
+    j.tuned_emax = p->tuned_emax;
     j.npass = (int)p->radix.size();
     for (int i = 0; i < j.npass && i < 40; i++) j.radix[i] = p->radix[i];
     j.lp = p->lp;

@@ -418,6 +418,10 @@ template <typename T> struct SmemArgs {
     // rows of the input view (tmap), tma_boxes per tile, tma_bytes in all
     int tma, tma_boxes, tma_rows;
     unsigned tma_bytes;
+    // test hook (jvsip_gpu_test_wait_expiry): after the boxes have landed,
+    // wait on the barrier's next phase, which nothing completes, so the
+    // bounded wait runs out with no copy in flight
+    int tma_expire;
     int *status;      // set to 1 when the bounded wait for the boxes expired
     // c2c tiles of column-type views: ld_rows / st_rows load / store with
     // consecutive threads on consecutive elements of one transform (the view
@@ -1002,7 +1006,8 @@ __global__ void __launch_bounds__(MAXT) k_smem(const __grid_constant__ SmemArgs<
                         tc::tma_load_2d(s + (size_t)i * a.tma_rows * a.vpb, &a.tmap, (int)(2 * v0),
                                         i * a.tma_rows, &tbar);
                 }
-                const bool got = __syncthreads_and(tc::mbar_wait(&tbar, 0, 1u << 24));
+                bool got = __syncthreads_and(tc::mbar_wait(&tbar, 0, 1u << 24));
+                if (got && a.tma_expire) got = __syncthreads_and(tc::mbar_wait(&tbar, 1, 1u << 12));
                 if (!got) {
                     if (tid == 0) atomicExch(a.status, 1);
                     return;

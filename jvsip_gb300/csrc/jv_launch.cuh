@@ -136,6 +136,7 @@ static bool tma_columns(SmemArgs<T> &a, const Job &j, long vpb, long ld) {
     a.tma_boxes = (int)nb;
     a.tma_rows = (int)rows;
     a.tma_bytes = (unsigned)(nb * rows * vpb * 2 * sizeof(T));
+    a.tma_expire = test_wait_expiry() ? 1 : 0;
     a.status = status;
     return true;
 }
@@ -346,6 +347,7 @@ bool launch_smem_t(const Job &j, cudaStream_t st) {
         vpb = target / N;
         if (vpb < 1) vpb = 1;
     }
+    if (j.tuned_vpb > 0) vpb = j.tuned_vpb;  // the autotuner's transforms per CTA (bounded below)
     size_t cap = d->smem_optin - kStaticSmem;
     while (vpb > 1 && ((size_t)vpb * ld * sizeof(C) > cap || vpb * N > elem_cap ||
                        threads_needed<K::EMAX_L>(j, vpb * N) > K::MAXT_L))
@@ -355,7 +357,9 @@ bool launch_smem_t(const Job &j, cudaStream_t st) {
         set_error(E_UNSUPPORTED, "length too large for the shared-memory kernel");
         return false;
     }
-    if (threads_needed<K::EMAX_S>(j, vpb * N) <= K::MAXT_S)
+    // 8 values per thread and pass when the threads suffice, else 16 (the
+    // autotuner may ask for 16 where 8 would fit)
+    if (j.tuned_emax != K::EMAX_L && threads_needed<K::EMAX_S>(j, vpb * N) <= K::MAXT_S)
         return launch_smem_v<T, KIND, K::EMAX_S, K::MAXT_S>(a, j, vpb, ld, st);
     return launch_smem_v<T, KIND, K::EMAX_L, K::MAXT_L>(a, j, vpb, ld, st);
 }

@@ -21,6 +21,7 @@
 #include <mutex>
 #include <new>
 #include <set>
+#include <string>
 #include <tuple>
 
 #include "jv_core.h"
@@ -172,6 +173,61 @@ std::vector<int> pass_radices(long N, bool *smooth, long maxt) {
     return r;
 }
 
+bool schedule_valid(const std::vector<int> &r, long N, long maxt) {
+    if (N < 2 || r.empty()) return false;
+    const long need = (N + maxt - 1) / maxt;
+    long prod = 1;
+    for (int R : r) {
+        if (!gpass_codelet_host(R) || (long)R * pass_k(16, R) < need) return false;
+        prod *= R;
+        if (prod > N) return false;
+    }
+    return prod == N;
+}
+
+// every multiset of usable codelet radices with product N and at most `maxp`
+// passes, each as a descending list
+static void schedules_rec(long n, int from, long need, int maxp, std::vector<int> &cur,
+                          std::vector<std::vector<int>> &out) {
+    if (n == 1) {
+        out.push_back(cur);
+        return;
+    }
+    if ((int)cur.size() >= maxp) return;
+    for (int i = from; i < kRadices; i++) {
+        const int R = kRadixList[i];
+        if (n % R || (long)R * pass_k(16, R) < need) continue;
+        cur.push_back(R);
+        schedules_rec(n / R, i, need, maxp, cur, out);
+        cur.pop_back();
+    }
+}
+
+std::vector<std::vector<int>> schedule_candidates(long N, long maxt, size_t limit) {
+    std::vector<std::vector<int>> out;
+    bool smooth = true;
+    std::vector<int> def = pass_radices(N, &smooth, maxt);
+    if (!smooth || !schedule_valid(def, N, maxt)) return out;
+    out.push_back(def);
+    std::vector<std::vector<int>> sets;
+    std::vector<int> cur;
+    schedules_rec(N, 0, (N + maxt - 1) / maxt, (int)def.size() + 1, cur, sets);
+    // fewer passes first; within a pass count larger radices first
+    std::stable_sort(sets.begin(), sets.end(), [](const std::vector<int> &a, const std::vector<int> &b) {
+        return a.size() != b.size() ? a.size() < b.size() : a > b;
+    });
+    auto add = [&](const std::vector<int> &c) {
+        if (out.size() < limit && std::find(out.begin(), out.end(), c) == out.end()) out.push_back(c);
+    };
+    for (const std::vector<int> &m : sets) {
+        add(m);                                  // descending
+        std::vector<int> asc(m.rbegin(), m.rend());
+        add(asc);                                // ascending
+        if (out.size() >= limit) break;
+    }
+    return out;
+}
+
 // exp(-2 pi i m/N) in double with the angle reduced to [0, pi] by symmetry
 static void unit_root(long m, long N, double *c, double *s) {
     bool flip = false;
@@ -193,7 +249,15 @@ struct TableSet {
     int refs = 0;
 };
 static std::mutex g_tab_mu;
-static std::map<std::tuple<long, int, int>, TableSet> g_tabs;
+static std::map<std::tuple<long, int, int, std::string>, TableSet> g_tabs;
+
+// the per-pass tables depend on the pass schedule: plans of one length with
+// different (tuned) schedules keep separate tables
+static std::string sched_key(const std::vector<int> &r) {
+    std::string k;
+    for (int R : r) k += std::to_string(R) + ",";
+    return k;
+}
 
 static int table_kind(int type) { return type == JV_RCFFTOP ? 1 : type == JV_CRFFTOP ? 2 : 0; }
 
@@ -202,7 +266,7 @@ static bool build_tables(Plan *p);
 
 template <typename T>
 static bool make_tables(Plan *p) {
-    auto key = std::make_tuple(p->MN, p->prec, table_kind(p->type));
+    auto key = std::make_tuple(p->MN, p->prec, table_kind(p->type), sched_key(p->radix));
     std::lock_guard<std::mutex> lk(g_tab_mu);
     auto it = g_tabs.find(key);
     if (it != g_tabs.end()) {
@@ -228,7 +292,7 @@ static bool make_tables(Plan *p) {
 
 static void release_tables(Plan *p) {
     std::lock_guard<std::mutex> lk(g_tab_mu);
-    auto key = std::make_tuple(p->MN, p->prec, table_kind(p->type));
+    auto key = std::make_tuple(p->MN, p->prec, table_kind(p->type), sched_key(p->radix));
     auto it = g_tabs.find(key);
     if (it != g_tabs.end() && it->second.tw == p->d_tw) {
         if (--it->second.refs > 0) return;
@@ -560,7 +624,20 @@ static Plan *new_plan(int type, vsip_length M, vsip_length N, double scale, int 
     }
     p->ntimes = ntimes;
     p->hint = (int)hint;
-    p->radix = pass_radices(p->MN, &p->smooth, p->prec == P_F32 ? 1024 : 512);
+    const long maxt = p->prec == P_F32 ? 1024 : 512;
+    p->radix = pass_radices(p->MN, &p->smooth, maxt);
+    {
+        // the autotuner's choice for this length, precision and stride class
+        PlainTune t;
+        if ((type == JV_CCFFTOP || type == JV_CCFFTIP) && p->smooth &&
+            plain_tuned(p->MN, p->prec, p->major, &t)) {
+            if (schedule_valid(t.radix, p->MN, maxt)) p->radix = t.radix;
+            if (t.res == 1) p->no_fast = true;
+            p->tuned_vpb = t.vpb;
+            p->tuned_emax = t.emax;
+            p->tuned = true;
+        }
+    }
     if (!direct_sum_ok(p)) {
         delete p;
         return nullptr;

@@ -2,8 +2,8 @@
 // products with hi/lo-split 16-bit operands and FP32 accumulation.
 //
 // A row x (n = 32a + b) is a 32 x 32 matrix X[a][b].  Its DFT is the
-// four-step  Z = F32^T-applied over a,  Z'[c][b] = Z[c][b] * w1024^(bc),
-// X[c + 32d] = sum_b Z'[c][b] w32^(bd).  Each step is a real GEMM whose A
+// four-step  Z[b][c] = sum_a X[a][b] w32^(ac),  Z'[b][c] = Z[b][c] w1024^(bc),
+// X[c + 32d] = sum_b Z'[b][c] w32^(bd).  Each step is a real GEMM whose A
 // operand is 128 x 128 (4 rows x 32 vectors; K = {hi, lo} x {re, im} x 32)
 // and whose B operand is 64 x 128 (the 32-point DFT matrix in the 2x2 real
 // form of complex multiplication, K = {W_hi, W_lo} x {re, im} x 32).  Three
@@ -11,16 +11,29 @@
 //     X_hi * W_hi  +  X_lo * W_hi  +  X_hi * W_lo
 // (A K-blocks 0-3 with B 0-3, A 4-7 with B 0-3, A 0-3 with B 4-7), which
 // recovers about 22 (FP16) or 16 (BF16) significant bits of each operand.
-// FP16 operands are scaled per row by a power of two before the split (so
-// their range fits FP16); BF16 operands are not scaled.  The inverse
-// direction runs as conj(F(conj x)); the user scale is applied at the store.
+// FP16 operands are scaled per row by a power of two before step 1 (the row's
+// largest component into [2^13, 2^14)) and by the fixed 2^-4 before step 2
+// (|Z'| <= 32 sqrt(2) 2^14, so the scaled values stay below FP16's maximum);
+// BF16 operands are not scaled.  The inverse direction runs as
+// conj(F(conj x)); the user scale and the inverse of the operand scales are
+// applied at the store.
 //
-// Per CTA: 128 threads, one warp per row; 64 tensor-memory columns hold the
-// 128 x 64 FP32 accumulator of step 1 and then of step 2; one elected thread
-// issues 12 tcgen05.mma per step and commits them to an mbarrier the CTA
-// waits on with a bounded loop.  The A operand's K-blocks are 2064 bytes
-// apart (2048 + 16) so that the step-2 stores, which run along K, spread
-// over all shared-memory banks.
+// The kernel is persistent: one 1024-thread CTA per SM holding four
+// independent row groups (8 warps each: warp q takes row q % 4 of the group
+// and the half q / 4 of its vectors or outputs), one 32 KB A operand and 64
+// tensor-memory columns per group, and one B operand for the CTA (16 KB, a
+// bulk copy at the start).  A group loops over groups of 4 rows; rows are read
+// from and written to global memory directly by coalesced per-lane accesses
+// (lane = vector b on the way in, output c on the way out), and the next
+// group's rows are prefetched into L2 at the start of each iteration.  Step
+// 1's operand is K-major (a lane writes 16-byte chunks of 8 consecutive a);
+// step 2's is MN-major (a lane holds Z'[b][c] for 16 consecutive c, written
+// as 16-byte chunks of 8 consecutive c), so no lane exchanges are needed.
+// One elected thread per group issues the 12 tcgen05.mma of a step and
+// commits them to the group's mbarrier; the group's warps synchronise on a
+// named barrier.  Every wait is bounded; on expiry the kernel records a
+// status that the next synchronisation reports (E_DEVICE), waits (bounded)
+// for MMAs and copies still in flight and frees its tensor memory.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <stdint.h>
@@ -39,19 +52,32 @@ namespace jv {
 
 constexpr int SPN = 1024;                        // transform length of the form
 constexpr int SPM = 128;                         // GEMM M: 4 rows x 32
-constexpr int SPK = 128;                         // operand K: {hi, lo} x {re, im} x 32
 constexpr int SPNN = 64;                         // GEMM N: {re, im} x 32
-constexpr uint32_t SP_A_LBO = (SPM / 8) * 128 + 16;  // bytes between K-adjacent core matrices of A
-constexpr uint32_t SP_B_LBO = (SPNN / 8) * 128;      // the same for B (unpadded)
-constexpr int SP_A_BYTES = (SPK / 8) * SP_A_LBO;     // 33024
-constexpr int SP_B_BYTES = (SPK / 8) * SP_B_LBO;     // 16384
-constexpr int SP_TMEM_COLS = 64;
+constexpr uint32_t SP_B_LBO = (SPNN / 8) * 128;  // B: bytes between K-adjacent core matrices
+constexpr int SP_B_BYTES = 16 * SP_B_LBO;        // 16384
+constexpr uint32_t SQ_KS = 128;                  // A: bytes between K-adjacent core matrices
+constexpr uint32_t SQ_MS = 2048;                 // A: bytes between M-adjacent core matrices
+constexpr int SQ_A_BYTES = 16 * SQ_MS;           // 32768 per group
+constexpr int SQG = 4;                           // row groups per CTA
+constexpr int SQW = 8;                           // warps per row group
+constexpr int SQ_THREADS = SQG * SQW * 32;       // 1024
+constexpr int SQ_TMEM_COLS = SQG * SPNN;         // 256
+constexpr int SQ_TW_BYTES = 32 * 32 * 8;         // the [c][b] twiddle table
 constexpr uint32_t SP_WAIT_LIMIT = 1u << 24;
 
 // byte offset of element (row, k) of a K-major no-swizzle operand made of
 // 8-row x 16-byte core matrices: [k/8] (lbo apart) [row/8] (128 apart) [row%8][k%8]
 __host__ __device__ __forceinline__ uint32_t core_off(int row, int k, uint32_t lbo) {
     return (uint32_t)(k >> 3) * lbo + (uint32_t)((row >> 3) << 7) + (uint32_t)((row & 7) << 4) + (uint32_t)((k & 7) << 1);
+}
+// A operand element (m, k): K-major for step 1 (core matrix = 8 rows m x 8
+// consecutive k), MN-major for step 2 (core matrix = 8 k x 8 consecutive m);
+// core matrices SQ_MS apart along m and SQ_KS apart along k in both
+__host__ __device__ __forceinline__ uint32_t a_off_k(int m, int k) {
+    return (uint32_t)(m >> 3) * SQ_MS + (uint32_t)(k >> 3) * SQ_KS + (uint32_t)((m & 7) << 4) + (uint32_t)((k & 7) << 1);
+}
+__host__ __device__ __forceinline__ uint32_t a_off_mn(int m, int k) {
+    return (uint32_t)(m >> 3) * SQ_MS + (uint32_t)(k >> 3) * SQ_KS + (uint32_t)((k & 7) << 4) + (uint32_t)((m & 7) << 1);
 }
 
 struct SplitArgs {
@@ -62,10 +88,8 @@ struct SplitArgs {
     int inv, has_scale;
     float scale;
     const uint4 *bop;     // B operand, SP_B_BYTES in core-matrix layout
-    const float2 *tw;     // [c][b] = exp(-2 pi i bc/1024), c, b < 32
+    const float2 *tw;     // [c][b] = s2 exp(-2 pi i bc/1024), c, b < 32 (s2: the step 2 operand scale)
     int *status;          // set to 1 when a barrier wait expired
-    int bulk_rows;        // input rows start on 16-byte boundaries: loaded by bulk copies
-    int bulk_out;         // output rows start on 16-byte boundaries: stored by bulk copies
 };
 
 // two floats -> one 32-bit word of two 16-bit values (first in the low half),
@@ -101,266 +125,239 @@ __device__ __forceinline__ void split2(float x0, float x1, uint32_t &hi, uint32_
     lo = pack2<BF>(x0 - f.x, x1 - f.y);
 }
 
-// power-of-two scale bringing the warp's largest magnitude into [2^13, 2^14)
-__device__ __forceinline__ float warp_scale(float m) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+// power of two bringing m (a row's largest component) into [2^13, 2^14)
+__device__ __forceinline__ float row_scale(float m) {
     if (!(m > 0.f) || !isfinite(m)) return 1.f;
-    int e = ilogbf(m);
-    return ldexpf(1.f, 13 - e);
+    return ldexpf(1.f, 13 - ilogbf(m));
 }
 
-// the three products of one step into tensor memory at `d`
-__device__ __forceinline__ void split_mma(uint32_t d, uint32_t a0, uint32_t b0, uint32_t idesc) {
-#pragma unroll 1
+__device__ __forceinline__ float warp_max(float m) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    return m;
+}
+
+// named barrier of `n` threads; the second form returns the AND of v over them
+__device__ __forceinline__ void bar_sync(int id, int n) {
+    asm volatile("bar.sync %0, %1;" :: "r"(id), "r"(n) : "memory");
+}
+__device__ __forceinline__ bool bar_and(int id, int n, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.and.pred q, %2, %3, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r) : "r"((uint32_t)v), "r"(id), "r"(n) : "memory");
+    return r != 0;
+}
+
+__device__ __forceinline__ void prefetch_l2(const void *p) {
+    asm volatile("{\n\t.reg .u64 a;\n\tcvta.to.global.u64 a, %0;\n\tprefetch.global.L2 [a];\n\t}" :: "l"(p));
+}
+
+__device__ __forceinline__ void sts128(unsigned char *p, uint32_t x, uint32_t y, uint32_t z, uint32_t w) {
+    *reinterpret_cast<uint4 *>(p) = make_uint4(x, y, z, w);
+}
+
+// the three products of one step into tensor memory at `d`; da / db are the
+// descriptors of the operands' first K chunks (a chunk of 16 k is 2 * SQ_KS
+// bytes further in A and 2 * SP_B_LBO in B: the address field counts 16 bytes)
+__device__ __forceinline__ void split_mma(uint32_t d, uint64_t da, uint64_t db, uint32_t idesc) {
+#pragma unroll
     for (int i = 0; i < 12; i++) {
         const int ka = (i < 8) ? i : i - 8;  // A K-chunk: hi 0-3, lo 4-7, hi 0-3
         const int kb = (i < 4) ? i : i - 4;  // B K-chunk: W_hi 0-3, W_hi 0-3, W_lo 4-7
-        tc::mma_f16(d, tc::smem_desc(a0 + ka * 2 * SP_A_LBO, SP_A_LBO, 128),
-                    tc::smem_desc(b0 + kb * 2 * SP_B_LBO, SP_B_LBO, 128), idesc, i > 0);
+        tc::mma_f16(d, da + (uint64_t)(ka * 2 * SQ_KS / 16), db + (uint64_t)(kb * 2 * SP_B_LBO / 16), idesc, i > 0);
     }
 }
 
-// 32 accumulator columns of this warp's lanes, from column `col`
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-    float t[16];
-    tc::tmem_ld16(taddr, t);
-#pragma unroll
-    for (int i = 0; i < 16; i++) v[i] = t[i];
-    tc::tmem_ld16(taddr + 16, t);
-#pragma unroll
-    for (int i = 0; i < 16; i++) v[16 + i] = t[i];
-}
-
-// ---- the steps of one group of 4 rows, shared by both kernels
-
-// step 1 operand from the thread's vector b = l of row w (v[a] = x[32a + l],
-// scaled by s1): A1[(w, b)][part*64 + ri*32 + a], K-blocks ab (re hi), 4+ab
-// (im hi), 8+ab (re lo), 12+ab (im lo)
-template <bool BF>
-__device__ __forceinline__ void sp_operand1(unsigned char *Asm, int w, int l, const float2 (&v)[32], float s1) {
-    unsigned char *arow = Asm + core_off(w * 32 + l, 0, SP_A_LBO);
-#pragma unroll
-    for (int ab = 0; ab < 4; ab++) {
-        uint4 hr, hi, lr, li;
-        uint32_t *phr = &hr.x, *phi = &hi.x, *plr = &lr.x, *pli = &li.x;
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const float2 e0 = v[ab * 8 + 2 * q], e1 = v[ab * 8 + 2 * q + 1];
-            split2<BF>(e0.x * s1, e1.x * s1, phr[q], plr[q]);
-            split2<BF>(e0.y * s1, e1.y * s1, phi[q], pli[q]);
-        }
-        *reinterpret_cast<uint4 *>(arow + (0 + ab) * SP_A_LBO) = hr;
-        *reinterpret_cast<uint4 *>(arow + (4 + ab) * SP_A_LBO) = hi;
-        *reinterpret_cast<uint4 *>(arow + (8 + ab) * SP_A_LBO) = lr;
-        *reinterpret_cast<uint4 *>(arow + (12 + ab) * SP_A_LBO) = li;
-    }
-}
-
-// step 1 result (lane (w, l) = (row, b), columns re c | im c) times the
-// twiddle w1024^(b c), then the step 2 operand A2[(w, c)][part*64 + ri*32 + b]
-// written over step 1's; returns the step's power-of-two scale.  Lane pairs
-// (l, l^1) trade one word so that each lane stores two 4-byte pairs of
-// adjacent b: even lanes (re hi, im hi) at b = l, odd lanes (re lo, im lo) at
-// b = l - 1; the two stores are ordered so the even and odd halves of the
-// warp fall in different banks.
-template <bool BF>
-__device__ __forceinline__ float sp_operand2(unsigned char *Asm, int w, int l, float (&zr)[32], float (&zi)[32],
-                                             const float2 *__restrict__ tw) {
-    float mx = 0.f;
-#pragma unroll
-    for (int c = 0; c < 32; c++) {
-        const float2 t = __ldg(&tw[c * 32 + l]);
-        const float r = zr[c] * t.x - zi[c] * t.y, i = zr[c] * t.y + zi[c] * t.x;
-        zr[c] = r;
-        zi[c] = i;
-        mx = fmaxf(mx, fmaxf(fabsf(r), fabsf(i)));
-    }
-    const float s2 = BF ? 1.f : warp_scale(mx);
-    const bool even = (l & 1) == 0;
-    const int k1 = even ? l : 96 + l - 1, k2 = even ? 32 + l : 64 + l - 1;
-    unsigned char *p1 = Asm + core_off(w * 32, k1, SP_A_LBO);
-    unsigned char *p2 = Asm + core_off(w * 32, k2, SP_A_LBO);
-#pragma unroll
-    for (int c = 0; c < 32; c++) {
-        uint32_t P, Q;  // (re hi | im hi << 16), (re lo | im lo << 16)
-        split2<BF>(zr[c] * s2, zi[c] * s2, P, Q);
-        const uint32_t R = __shfl_xor_sync(0xffffffffu, even ? Q : P, 1);
-        const uint32_t X = even ? P : R, Y = even ? R : Q;
-        const uint32_t wlo = __byte_perm(X, Y, 0x5410), whi = __byte_perm(X, Y, 0x7632);
-        const uint32_t mo = (uint32_t)((c >> 3) << 7) + (uint32_t)((c & 7) << 4);
-        *reinterpret_cast<uint32_t *>(p1 + mo) = even ? wlo : whi;
-        *reinterpret_cast<uint32_t *>(p2 + mo) = even ? whi : wlo;
-    }
-    return s2;
-}
-
-// step 2 result: lane (w, l) = (row, c = l), columns re d | im d -> out[c + 32 d]
-// With output rows on 16-byte boundaries the rows are staged in the A
-// operand's space (free once step 2's MMAs completed) and written by one bulk
-// copy each, issued by thread 0, which waits until the copies have read the
-// stage (the CTA's shared memory outlives them).
-__device__ __forceinline__ void sp_store(const SplitArgs &a, uint32_t lane_base, long row, int l, float f,
-                                         unsigned char *Asm, int tid) {
-    float yr[32], yi[32];
-    tmem_ld32(lane_base + 0, yr);
-    tmem_ld32(lane_base + 32, yi);
-    tc::tmem_ld_wait();
-    if (a.bulk_out) {
-        const int w = tid >> 5;
-        float2 *stg = reinterpret_cast<float2 *>(Asm) + w * SPN;
-#pragma unroll
-        for (int d = 0; d < 32; d++) {
-            float2 o = make_float2(yr[d] * f, yi[d] * f);
-            if (a.inv) o.y = -o.y;
-            stg[l + 32 * d] = o;
-        }
-        tc::fence_async_smem();
-        __syncthreads();
-        if (tid == 0) {
-            const long row0 = row - w;
-            const int nr = (int)min(4L, a.nvec - row0);
-            for (int r = 0; r < nr; r++)
-                tc::bulk_store(a.out + a.off_out + (row0 + r) * a.vs_out, Asm + r * SPN * 8, SPN * 8);
-            tc::bulk_commit();
-            tc::bulk_wait_read();
-        }
-        return;
-    }
-    if (row < a.nvec) {
-        float2 *dst = a.out + a.off_out + row * a.vs_out;
-#pragma unroll
-        for (int d = 0; d < 32; d++) {
-            float2 o = make_float2(yr[d] * f, yi[d] * f);
-            if (a.inv) o.y = -o.y;
-            dst[l + 32 * d] = o;
-        }
-    }
-}
-
-// Steps 1 and 2 of the group whose rows the threads hold in v (conjugated when
-// inverse): operand, MMAs, twiddle, operand, MMAs, store.  Returns false when
-// a barrier wait expired (uniform over the CTA); *pending is then the MMA
-// barrier phase still outstanding (2: none).
-template <bool BF>
-__device__ __forceinline__ bool sp_group(const SplitArgs &a, unsigned char *Asm, uint32_t a0, uint32_t b0,
-                                         uint32_t tbase, uint64_t *mbar, float2 (&v)[32], long row, int tid,
-                                         uint32_t *pending) {
-    const int w = tid >> 5, l = tid & 31;
-    float mx = 0.f;
-#pragma unroll
-    for (int i = 0; i < 32; i++) mx = fmaxf(mx, fmaxf(fabsf(v[i].x), fabsf(v[i].y)));
-    const float s1 = BF ? 1.f : warp_scale(mx);
-    sp_operand1<BF>(Asm, w, l, v, s1);
-    tc::fence_async_smem();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    const uint32_t idesc = tc::idesc_f16(SPM, SPNN, BF ? 1 : 0);
-    if (tid == 0) {
-        split_mma(tbase, a0, b0, idesc);
-        tc::mma_commit(mbar);
-    }
-    bool ok = tc::mbar_wait(mbar, 0, SP_WAIT_LIMIT);
-    ok = __syncthreads_and(ok);
-    *pending = ok ? 2u : 0u;
-    tc::fence_after_sync();
-    if (!ok) return false;
-    const uint32_t lane_base = tbase + ((uint32_t)(w * 32) << 16);
-    float zr[32], zi[32];
-    tmem_ld32(lane_base + 0, zr);
-    tmem_ld32(lane_base + 32, zi);
-    tc::tmem_ld_wait();
-    const float s2 = sp_operand2<BF>(Asm, w, l, zr, zi, a.tw);
-    // the step 1 accumulator is read out: step 2 reuses its columns
-    tc::fence_async_smem();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    if (tid == 0) {
-        split_mma(tbase, a0, b0, idesc);
-        tc::mma_commit(mbar);
-    }
-    ok = tc::mbar_wait(mbar, 1, SP_WAIT_LIMIT);
-    ok = __syncthreads_and(ok);
-    *pending = ok ? 2u : 1u;
-    tc::fence_after_sync();
-    if (!ok) return false;
-    sp_store(a, lane_base, row, l, (a.has_scale ? a.scale : 1.f) / (s1 * s2), Asm, tid);
-    // the accumulator is read out before the next group's step 1 writes it
-    tc::fence_before_sync();
-    return true;
-}
-
-// One group per CTA (any 8-byte aligned rows).
-template <bool BF>
-__global__ void __launch_bounds__(128, 4) k_split1024(const SplitArgs a) {
-    extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *Bsm = smem;                     // 16 KiB
-    unsigned char *Asm = smem + SP_B_BYTES;        // 33024 bytes
-    __shared__ __align__(8) uint64_t mbar, bbar, ibar;
-    __shared__ uint32_t tslot;
-    const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
-    const long row0 = (long)blockIdx.x * 4, row = row0 + w;
+// half h of row `row` (v[i] = x[32 (16h + i) + b], b = lane), conjugated for
+// the inverse; rows at or beyond nvec read as zeros
+__device__ __forceinline__ void load_half(const SplitArgs &a, long row, int h, int lane, float2 (&v)[16]) {
     const bool live = row < a.nvec;
-    const int nr = (int)min(4L, a.nvec - row0);
-    if (w == 0) {
-        tc::tmem_alloc(&tslot, SP_TMEM_COLS);
+    const float2 *src = a.in + a.off_in + (live ? row : 0) * a.vs_in + 512 * h + lane;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        float2 c = live ? src[32 * i] : make_float2(0.f, 0.f);
+        if (a.inv) c.y = -c.y;
+        v[i] = c;
+    }
+}
+
+// Persistent kernel: gridDim.x CTAs of SQG row groups; group slot s of CTA
+// blk processes the 4-row groups g = blk * SQG + s, stepping by gridDim.x * SQG.
+// The slot's next rows are prefetched into L2 at the start of each iteration.
+template <bool BF>
+__global__ void __launch_bounds__(SQ_THREADS, 1) k_split1024(const SplitArgs a) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bbar, mbar[SQG];
+    __shared__ uint32_t tslot;
+    __shared__ float smax[SQG][SQW];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int grp = warp / SQW, q = warp % SQW, r = q & 3, h = q >> 2;
+    const int gt = tid % (SQW * 32);               // thread index within the group
+    const int bar_id = 1 + grp, bar_n = SQW * 32;
+    unsigned char *Bsm = smem;
+    const float2 *tws = reinterpret_cast<const float2 *>(smem + SP_B_BYTES);
+    unsigned char *Asm = smem + SP_B_BYTES + SQ_TW_BYTES + grp * SQ_A_BYTES;
+    if (warp == 0) {
+        tc::tmem_alloc(&tslot, SQ_TMEM_COLS);
         tc::tmem_relinquish();
     }
     if (tid == 0) {
-        tc::mbar_init(&mbar, 1);
-        // the B operand (constant per plan) by one bulk copy, and with rows on
-        // 16-byte boundaries the group's rows by one bulk copy each into the A
-        // operand's space (free until step 1's operand is written)
+        for (int g = 0; g < SQG; g++) tc::mbar_init(&mbar[g], 1);
         tc::mbar_init(&bbar, 1);
-        tc::mbar_expect_tx(&bbar, SP_B_BYTES);
+        tc::mbar_expect_tx(&bbar, SP_B_BYTES + SQ_TW_BYTES);
         tc::bulk_load(Bsm, a.bop, SP_B_BYTES, &bbar);
-        if (a.bulk_rows) {
-            tc::mbar_init(&ibar, 1);
-            tc::mbar_expect_tx(&ibar, (uint32_t)(nr * SPN * 8));
-            for (int r = 0; r < nr; r++)
-                tc::bulk_load(Asm + r * SPN * 8, a.in + a.off_in + (row0 + r) * a.vs_in, SPN * 8, &ibar);
-        }
-    }
-    // thread (w, l) owns vector b = l of row w: x[32a + l], a < 32
-    float2 v[32];
-    bool ok = true;
-    if (a.bulk_rows) {
-        __syncthreads();  // the barrier is initialised
-        ok = tc::mbar_wait(&ibar, 0, SP_WAIT_LIMIT);
-        const float2 *src = reinterpret_cast<const float2 *>(Asm) + w * SPN;
-#pragma unroll
-        for (int i = 0; i < 32; i++) {
-            float2 c = (live && ok) ? src[32 * i + l] : make_float2(0.f, 0.f);
-            if (a.inv) c.y = -c.y;
-            v[i] = c;
-        }
-    } else {
-        const float2 *src = a.in + a.off_in + (live ? row : 0) * a.vs_in;
-#pragma unroll
-        for (int i = 0; i < 32; i++) {
-            float2 c = live ? src[32 * i + l] : make_float2(0.f, 0.f);
-            if (a.inv) c.y = -c.y;
-            v[i] = c;
-        }
-    }
-    tc::fence_before_sync();
-    ok = __syncthreads_and(ok);  // also: every thread has read its row from the A space
-    tc::fence_after_sync();
-    uint32_t pending = 2u;
-    if (!ok && a.bulk_rows) tc::mbar_wait(&ibar, 0, SP_WAIT_LIMIT);
-    ok = ok && __syncthreads_and(tc::mbar_wait(&bbar, 0, SP_WAIT_LIMIT));
-    if (ok) ok = sp_group<BF>(a, Asm, tc::smem_addr(Asm), tc::smem_addr(Bsm), tslot, &mbar, v, row, tid, &pending);
-    else tc::mbar_wait(&bbar, 0, SP_WAIT_LIMIT);  // the copy ends before the CTA's shared memory is released
-    if (!ok) {
-        if (tid == 0) atomicExch(a.status, 1);
-        // let MMAs still in flight finish (bounded) before the tensor memory is freed
-        if (pending < 2u) tc::mbar_wait(&mbar, pending, SP_WAIT_LIMIT);
+        tc::bulk_load(smem + SP_B_BYTES, a.tw, SQ_TW_BYTES, &bbar);
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (w == 0) tc::tmem_dealloc(tslot, SP_TMEM_COLS);
+    tc::fence_after_sync();
+    bool ok = tc::mbar_wait(&bbar, 0, SP_WAIT_LIMIT);
+    const uint32_t tmem = tslot + (uint32_t)(grp * SPNN);
+    // this warp's tensor-memory lanes: rows 32r..32r+31 of the group's tile
+    const uint32_t lane_addr = tmem + ((uint32_t)(r * 32) << 16);
+    const uint32_t idesc1 = tc::idesc_f16(SPM, SPNN, BF ? 1 : 0);
+    const uint32_t idesc2 = idesc1 | (1u << 15);  // A MN-major
+    const int ngroups = (int)((a.nvec + 3) / 4);  // nvec < 2^31 (checked by the launcher)
+    const int gstep = (int)gridDim.x * SQG;
+    const float s2 = BF ? 1.f : 0.0625f;  // folded into a.tw
+    uint32_t pending = 2u;  // parity of a committed MMA phase this thread has not seen complete (2: none)
+    for (int g = (int)blockIdx.x * SQG + grp; g < ngroups; g += gstep) {
+        const long row = (long)g * 4 + r;
+        {
+            // the slot's group after next into L2: 4 rows x 64 lines of 128 bytes
+            const long rn = ((long)g + gstep) * 4 + (gt >> 6);
+            if (rn < a.nvec) prefetch_l2(a.in + a.off_in + rn * a.vs_in + (gt & 63) * 16);
+        }
+        float2 v[16];
+        load_half(a, row, h, lane, v);
+        if (!BF) {
+            float mx = 0.f;
+#pragma unroll
+            for (int i = 0; i < 16; i++) mx = fmaxf(mx, fmaxf(fabsf(v[i].x), fabsf(v[i].y)));
+            mx = warp_max(mx);
+            if (lane == 0) smax[grp][q] = mx;
+        }
+        ok = bar_and(bar_id, bar_n, ok);
+        if (!ok) break;
+        const float s1 = BF ? 1.f : row_scale(fmaxf(smax[grp][r], smax[grp][r + 4]));
+        // step 1 operand A1[m = 32r + b][k = part*64 + ri*32 + a], K-major
+        {
+            const int m = 32 * r + lane;
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                uint32_t hr[4], hi[4], lr[4], li[4];
+#pragma unroll
+                for (int t = 0; t < 4; t++) {
+                    const float2 e0 = v[8 * j + 2 * t], e1 = v[8 * j + 2 * t + 1];
+                    split2<BF>(e0.x * s1, e1.x * s1, hr[t], lr[t]);
+                    split2<BF>(e0.y * s1, e1.y * s1, hi[t], li[t]);
+                }
+                const int ka = 16 * h + 8 * j;
+                sts128(Asm + a_off_k(m, ka), hr[0], hr[1], hr[2], hr[3]);
+                sts128(Asm + a_off_k(m, 32 + ka), hi[0], hi[1], hi[2], hi[3]);
+                sts128(Asm + a_off_k(m, 64 + ka), lr[0], lr[1], lr[2], lr[3]);
+                sts128(Asm + a_off_k(m, 96 + ka), li[0], li[1], li[2], li[3]);
+            }
+        }
+        tc::fence_async_smem();
+        tc::fence_before_sync();
+        bar_sync(bar_id, bar_n);
+        tc::fence_after_sync();
+        if (gt == 0) {
+            split_mma(tmem, tc::smem_desc(tc::smem_addr(Asm), SQ_KS, SQ_MS),
+                      tc::smem_desc(tc::smem_addr(Bsm), SP_B_LBO, 128), idesc1);
+            tc::mma_commit(&mbar[grp]);
+        }
+        pending = 0u;
+        ok = tc::mbar_wait(&mbar[grp], 0, SP_WAIT_LIMIT);
+        if (ok) pending = 2u;
+        tc::fence_after_sync();
+        // step 1 result (lane = b, columns re c | im c for c in half h) times
+        // s2 w1024^(bc) as the step 2 operand A2[m = 32r + c][k = part*64 + ri*32 + b], MN-major
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            float zr[8], zi[8];
+            if (ok) {
+                tc::tmem_ld8(lane_addr + 16 * h + 8 * j, zr);
+                tc::tmem_ld8(lane_addr + 32 + 16 * h + 8 * j, zi);
+                tc::tmem_ld_wait();
+            } else {
+#pragma unroll
+                for (int i = 0; i < 8; i++) zr[i] = zi[i] = 0.f;
+            }
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const float2 t = tws[(16 * h + 8 * j + i) * 32 + lane];
+                const float re = zr[i] * t.x - zi[i] * t.y, im = zr[i] * t.y + zi[i] * t.x;
+                zr[i] = re;
+                zi[i] = im;
+            }
+            uint32_t hr[4], hi[4], lr[4], li[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                split2<BF>(zr[2 * t], zr[2 * t + 1], hr[t], lr[t]);
+                split2<BF>(zi[2 * t], zi[2 * t + 1], hi[t], li[t]);
+            }
+            const int mc = 32 * r + 16 * h + 8 * j;
+            sts128(Asm + a_off_mn(mc, lane), hr[0], hr[1], hr[2], hr[3]);
+            sts128(Asm + a_off_mn(mc, 32 + lane), hi[0], hi[1], hi[2], hi[3]);
+            sts128(Asm + a_off_mn(mc, 64 + lane), lr[0], lr[1], lr[2], lr[3]);
+            sts128(Asm + a_off_mn(mc, 96 + lane), li[0], li[1], li[2], li[3]);
+        }
+        tc::fence_async_smem();
+        tc::fence_before_sync();
+        ok = bar_and(bar_id, bar_n, ok);
+        tc::fence_after_sync();
+        if (!ok) break;
+        pending = 2u;  // the step 1 products completed (every thread of the group saw it)
+        if (gt == 0) {
+            split_mma(tmem, tc::smem_desc(tc::smem_addr(Asm), SQ_KS, SQ_MS),
+                      tc::smem_desc(tc::smem_addr(Bsm), SP_B_LBO, 128), idesc2);
+            tc::mma_commit(&mbar[grp]);
+        }
+        pending = 1u;
+        ok = tc::mbar_wait(&mbar[grp], 1, SP_WAIT_LIMIT);
+        tc::fence_after_sync();
+        if (ok) {
+            pending = 2u;
+            // step 2 result: lane = c, columns re d | im d for d in half h -> out[c + 32d]
+            const float f = (a.has_scale ? a.scale : 1.f) / (s1 * s2);
+            const bool live = row < a.nvec;
+            float2 *dst = a.out + a.off_out + (live ? row : 0) * a.vs_out + 512 * h + lane;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                float yr[4], yi[4];
+                tc::tmem_ld4(lane_addr + 16 * h + 4 * j, yr);
+                tc::tmem_ld4(lane_addr + 32 + 16 * h + 4 * j, yi);
+                tc::tmem_ld_wait();
+                if (live) {
+#pragma unroll
+                    for (int i = 0; i < 4; i++) {
+                        float2 o = make_float2(yr[i] * f, yi[i] * f);
+                        if (a.inv) o.y = -o.y;
+                        dst[32 * (4 * j + i)] = o;
+                    }
+                }
+            }
+        }
+        // the next iteration's first barrier orders these tensor-memory reads
+        // before the next products overwrite the tile
+        tc::fence_before_sync();
+    }
+    if (!ok) {
+        atomicExch(a.status, 1);
+        // let MMAs and the B copy still in flight finish (bounded) before the
+        // tensor memory and the CTA's shared memory are released
+        if (pending < 2u) tc::mbar_wait(&mbar[grp], pending, SP_WAIT_LIMIT);
+        tc::mbar_wait(&bbar, 0, SP_WAIT_LIMIT);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tslot, SQ_TMEM_COLS);
 }
 
 // ---------------------------------------------------------------- host side
@@ -401,27 +398,31 @@ static std::vector<uint16_t> b_operand() {
 
 static std::mutex g_sp_mu;
 static void *g_bop[2] = {nullptr, nullptr};
-static void *g_tw = nullptr;
+static void *g_tw[2] = {nullptr, nullptr};  // [c][b] twiddles times 2^-4 (FP16 form), times 1 (BF16 form)
 static int *g_status = nullptr;
 
 static bool split_tables() {
-    if (g_bop[0] && g_bop[1] && g_tw && g_status) return true;
+    if (g_bop[0] && g_bop[1] && g_tw[0] && g_tw[1] && g_status) return true;
     std::vector<uint16_t> b16 = b_operand<false>(), bbf = b_operand<true>();
-    std::vector<float> w(2 * 32 * 32);
+    std::vector<float> w(2 * 32 * 32), w16(2 * 32 * 32);
     for (int c = 0; c < 32; c++)
         for (int bb = 0; bb < 32; bb++) {
             double ang = -2.0 * 3.14159265358979323846264338327950288 * (double)(bb * c) / SPN;
             w[2 * (c * 32 + bb)] = (float)cos(ang);
             w[2 * (c * 32 + bb) + 1] = (float)sin(ang);
+            w16[2 * (c * 32 + bb)] = w[2 * (c * 32 + bb)] * 0.0625f;  // exact: a power of two
+            w16[2 * (c * 32 + bb) + 1] = w[2 * (c * 32 + bb) + 1] * 0.0625f;
         }
     g_bop[0] = dmalloc(SP_B_BYTES);
     g_bop[1] = dmalloc(SP_B_BYTES);
-    g_tw = dmalloc(w.size() * sizeof(float));
+    g_tw[0] = dmalloc(w.size() * sizeof(float));
+    g_tw[1] = dmalloc(w.size() * sizeof(float));
     g_status = (int *)dmalloc(sizeof(int));
-    if (!g_bop[0] || !g_bop[1] || !g_tw || !g_status) return false;
+    if (!g_bop[0] || !g_bop[1] || !g_tw[0] || !g_tw[1] || !g_status) return false;
     return cuda_ok(cudaMemcpy(g_bop[0], b16.data(), SP_B_BYTES, cudaMemcpyHostToDevice), "split tables") &&
            cuda_ok(cudaMemcpy(g_bop[1], bbf.data(), SP_B_BYTES, cudaMemcpyHostToDevice), "split tables") &&
-           cuda_ok(cudaMemcpy(g_tw, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice), "split tables") &&
+           cuda_ok(cudaMemcpy(g_tw[0], w16.data(), w16.size() * sizeof(float), cudaMemcpyHostToDevice), "split tables") &&
+           cuda_ok(cudaMemcpy(g_tw[1], w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice), "split tables") &&
            cuda_ok(cudaMemset(g_status, 0, sizeof(int)), "split status");
 }
 
@@ -452,15 +453,18 @@ bool launch_split_f32(const Job &j, cudaStream_t st) {
     a.has_scale = j.has_scale;
     a.scale = (float)j.scale;
     a.bop = (const uint4 *)g_bop[bf ? 1 : 0];
-    a.tw = (const float2 *)g_tw;
+    a.tw = (const float2 *)g_tw[bf ? 1 : 0];
     a.status = g_status;
-    // operand reads: A chunks start at 2 * ka * SP_A_LBO (ka < 8) and span two
-    // K-blocks of 16 x 128 bytes, ending at byte 16 * SP_A_LBO - 17 of A; B
-    // chunks end at byte 16 * SP_B_LBO - 1 of B: both inside their operands
+    // operand reads: A chunks start at 2 * ka * SQ_KS (ka < 8) and span 16
+    // core matrices along m (SQ_MS apart) and 2 along k, ending at byte
+    // 14 * SQ_KS + 15 * SQ_MS + 2 * SQ_KS - 1 < SQ_A_BYTES of the group's A
+    // (whichever of the two descriptor strides is taken along m); B chunks
+    // end at byte 16 * SP_B_LBO - 1 of B: all inside the operands
     const long ngroups = (j.nvec + 3) / 4;
-    a.bulk_rows = ((uintptr_t)ci.re % 16) == 0 && (ci.off % 2) == 0 && (j.nvec == 1 || (ci.vs % 2) == 0);
-    a.bulk_out = ((uintptr_t)co.re % 16) == 0 && (co.off % 2) == 0 && (j.nvec == 1 || (co.vs % 2) == 0);
-    const size_t smem = SP_A_BYTES + SP_B_BYTES;
+    Device *d = device();
+    long grid = (ngroups + SQG - 1) / SQG;
+    if (grid > d->sms) grid = d->sms;
+    const size_t smem = SP_B_BYTES + SQ_TW_BYTES + SQG * SQ_A_BYTES;
     static std::atomic<bool> attr[2]{};  // set once per form; concurrent first calls both set it
     if (!attr[bf]) {
         cudaError_t e = bf ? cudaFuncSetAttribute(k_split1024<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
@@ -468,8 +472,8 @@ bool launch_split_f32(const Job &j, cudaStream_t st) {
         if (!cuda_ok(e, "cudaFuncSetAttribute")) return true;
         attr[bf] = true;
     }
-    if (bf) k_split1024<true><<<(unsigned)ngroups, 128, smem, st>>>(a);
-    else k_split1024<false><<<(unsigned)ngroups, 128, smem, st>>>(a);
+    if (bf) k_split1024<true><<<(unsigned)grid, SQ_THREADS, smem, st>>>(a);
+    else k_split1024<false><<<(unsigned)grid, SQ_THREADS, smem, st>>>(a);
     count_launch();
     cuda_ok(cudaGetLastError(), "k_split1024 launch");
     return true;

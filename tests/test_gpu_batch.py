@@ -99,6 +99,15 @@ def test_batch_equals_per_plan_calls():
     assert np.linalg.norm(y - loop) / np.linalg.norm(loop) < 1e-6
 
 
+def test_loop_from_c_equals_per_plan_calls():
+    L = J.lib()
+    x, y, bx, by, plans, vin, vout, offs, (P, VI, VO) = make_batch(SEQ[:12], seed=5)
+    assert L.jvsip_fftm_loop_f(12, P, VI, VO) == 0, J.last_error()
+    by.sync()
+    oracle_check(SEQ[:12], x, y, offs)
+    assert L.jvsip_fftm_loop_f(0, None, None, None) == 0
+
+
 def test_batch_rejects_unsupported():
     L = J.lib()
     x = np.zeros(2 * 64 * 11, np.float32)
