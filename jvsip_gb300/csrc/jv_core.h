@@ -282,8 +282,9 @@ struct PlainTune {
 bool plain_tuned(long N, int prec, int cls, PlainTune *out);  // the forced or cached entry
 void plain_tune_force(const PlainTune *t);  // this thread's plans use t instead of the cache (nullptr: off)
 // Schedules of the shared-memory kernel for N (2^a 3^b 5^c 7^d): the default
-// (fewest passes, largest radices first) first, then other orders and
-// decompositions with at most one pass more; at most `limit` of them.
+// (fewest passes, largest radices first) first, then the other decompositions
+// into codelet radices with at most one pass more, each largest first (the
+// kernel runs its codelets in that order); at most `limit` of them.
 std::vector<std::vector<int>> schedule_candidates(long N, long maxt, size_t limit);
 bool schedule_valid(const std::vector<int> &r, long N, long maxt);
 

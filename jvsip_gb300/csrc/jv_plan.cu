@@ -177,7 +177,10 @@ bool schedule_valid(const std::vector<int> &r, long N, long maxt) {
     if (N < 2 || r.empty()) return false;
     const long need = (N + maxt - 1) / maxt;
     long prod = 1;
-    for (int R : r) {
+    for (size_t i = 0; i < r.size(); i++) {
+        const int R = r[i];
+        // the shared-memory kernel runs its codelets largest first
+        if (i && R > r[i - 1]) return false;
         if (!gpass_codelet_host(R) || (long)R * pass_k(16, R) < need) return false;
         prod *= R;
         if (prod > N) return false;
@@ -220,9 +223,7 @@ std::vector<std::vector<int>> schedule_candidates(long N, long maxt, size_t limi
         if (out.size() < limit && std::find(out.begin(), out.end(), c) == out.end()) out.push_back(c);
     };
     for (const std::vector<int> &m : sets) {
-        add(m);                                  // descending
-        std::vector<int> asc(m.rbegin(), m.rend());
-        add(asc);                                // ascending
+        add(m);  // descending: the kernel's codelet order
         if (out.size() >= limit) break;
     }
     return out;
