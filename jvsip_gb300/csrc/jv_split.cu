@@ -25,9 +25,9 @@
 // table for the CTA (16 + 8 KB, bulk copies at the start).  A group loops over
 // groups of 4 rows; rows are read from and written to global memory directly
 // by coalesced per-lane accesses (lane = vector b on the way in, output c on
-// the way out); a group's rows are prefetched into L2 two iterations ahead
-// and loaded into registers one iteration ahead, while the previous group's
-// step 2 products run and its outputs are stored.  Step
+// the way out), and the group's next rows are prefetched into L2 at the start
+// of each iteration.  (Loading them into registers one iteration ahead was
+// measured slower: the extra live registers spill at 64 per thread.)  Step
 // 1's operand is K-major (a lane writes 16-byte chunks of 8 consecutive a);
 // step 2's is MN-major (a lane holds Z'[b][c] for 16 consecutive c, written
 // as 16-byte chunks of 8 consecutive c), so no lane exchanges are needed.
@@ -189,10 +189,7 @@ __device__ __forceinline__ void load_half(const SplitArgs &a, long row, int h, i
 
 // Persistent kernel: gridDim.x CTAs of SQG row groups; group slot s of CTA
 // blk processes the 4-row groups g = blk * SQG + s, stepping by gridDim.x * SQG.
-// The slot's group after next is prefetched into L2 at the start of each
-// iteration, and its next rows are loaded into registers as soon as the
-// step 2 products are issued, so the loads complete while the products run
-// and the outputs are stored.
+// The slot's next rows are prefetched into L2 at the start of each iteration.
 template <bool BF>
 __global__ void __launch_bounds__(SQ_THREADS, 1) k_split1024(const SplitArgs a) {
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -230,16 +227,15 @@ __global__ void __launch_bounds__(SQ_THREADS, 1) k_split1024(const SplitArgs a) 
     const int gstep = (int)gridDim.x * SQG;
     const float s2 = BF ? 1.f : 0.0625f;  // folded into a.tw
     uint32_t pending = 2u;  // parity of a committed MMA phase this thread has not seen complete (2: none)
-    int g = (int)blockIdx.x * SQG + grp;
-    float2 v[16];
-    if (g < ngroups) load_half(a, (long)g * 4 + r, h, lane, v);
-    for (; g < ngroups; g += gstep) {
+    for (int g = (int)blockIdx.x * SQG + grp; g < ngroups; g += gstep) {
         const long row = (long)g * 4 + r;
         {
             // the slot's group after next into L2: 4 rows x 64 lines of 128 bytes
-            const long rn = ((long)g + 2 * gstep) * 4 + (gt >> 6);
+            const long rn = ((long)g + gstep) * 4 + (gt >> 6);
             if (rn < a.nvec) prefetch_l2(a.in + a.off_in + rn * a.vs_in + (gt & 63) * 16);
         }
+        float2 v[16];
+        load_half(a, row, h, lane, v);
         if (!BF) {
             float mx = 0.f;
 #pragma unroll
@@ -326,8 +322,6 @@ __global__ void __launch_bounds__(SQ_THREADS, 1) k_split1024(const SplitArgs a) 
             tc::mma_commit(&mbar[grp]);
         }
         pending = 1u;
-        // the slot's next rows, in flight while the products run
-        if (g + gstep < ngroups) load_half(a, ((long)g + gstep) * 4 + r, h, lane, v);
         ok = tc::mbar_wait(&mbar[grp], 1, SP_WAIT_LIMIT);
         tc::fence_after_sync();
         if (ok) {
@@ -337,17 +331,17 @@ __global__ void __launch_bounds__(SQ_THREADS, 1) k_split1024(const SplitArgs a) 
             const bool live = row < a.nvec;
             float2 *dst = a.out + a.off_out + (live ? row : 0) * a.vs_out + 512 * h + lane;
 #pragma unroll
-            for (int j = 0; j < 2; j++) {
-                float yr[8], yi[8];
-                tc::tmem_ld8(lane_addr + 16 * h + 8 * j, yr);
-                tc::tmem_ld8(lane_addr + 32 + 16 * h + 8 * j, yi);
+            for (int j = 0; j < 4; j++) {
+                float yr[4], yi[4];
+                tc::tmem_ld4(lane_addr + 16 * h + 4 * j, yr);
+                tc::tmem_ld4(lane_addr + 32 + 16 * h + 4 * j, yi);
                 tc::tmem_ld_wait();
                 if (live) {
 #pragma unroll
-                    for (int i = 0; i < 8; i++) {
+                    for (int i = 0; i < 4; i++) {
                         float2 o = make_float2(yr[i] * f, yi[i] * f);
                         if (a.inv) o.y = -o.y;
-                        dst[32 * (8 * j + i)] = o;
+                        dst[32 * (4 * j + i)] = o;
                     }
                 }
             }
