@@ -55,8 +55,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "batched FFT GB/s (% HBM peak): split-TC & batched vs plain FP32 at ≤1e-6 rel err"
 FALLBACK_HBM = 6800.0
-WORKLOADS = ["cfg3", "cfg1", "cfg2col", "cfg2rc", "cfg2cr", "cfg3d", "cfg4", "cfg5", "vec", "vecd", "vecrc", "cols",
-             "rows", "komega", "split"]
+WORKLOADS = ["cfg3", "cfg1", "cfg2col", "cfg2rc", "cfg2cr", "cfg3d", "cfg4", "cfg5", "vec", "vecd", "vecrc", "veccr",
+             "cols", "rows", "komega", "split", "primes"]
 
 
 def args():
@@ -396,10 +396,33 @@ def other_workload(a):
         call = lambda: L.vsip_ccfftmop_f(plan.h, vx.h, vy.h)
         nbytes, dt = 16 * tot, "f32"
         desc = f"vsip_ccfftmop_f {M}x{N} c64 VSIP_ROW, split complex blocks (cstride 1), N(0,1)"
-    elif w in ("vec", "vecd", "vecrc"):
-        # one single FFT of --points points (vsip_ccfftop / vsip_rcfftop)
+    elif w == "primes":
+        # a length with a prime factor above 7: 4096 rows of 5632 = 8 x 8 x 8 x 11 points
+        # (the multi-pass global path, the radix-11 pass a direct sum)
+        M, N = 4096, 5632
+        x = synth.fill(2 * M * N, 14, 1)
+        y = np.zeros_like(x)
+        plan = J.FFTM(J.KIND_CCOP, M, N, 1.0, -1, J.VSIP_ROW, ntimes=1)
+        bx, by = J.CBlock(x), J.CBlock(y)
+        vx, vy = bx.view(0, N, M, 1, N), by.view(0, N, M, 1, N)
+        call = lambda: L.vsip_ccfftmop_f(plan.h, vx.h, vy.h)
+        nbytes, dt = 16 * M * N, "f32"
+        desc = "vsip_ccfftmop_f 4096x5632 (8*8*8*11) c64 VSIP_ROW forward, N(0,1)"
+    elif w in ("vec", "vecd", "vecrc", "veccr"):
+        # one single FFT of --points points (vsip_ccfftop / vsip_rcfftop / vsip_crfftop)
         N = M = a.points
-        if w == "vecrc":
+        if w == "veccr":
+            # C2R of N/2+1 bins into a real vector of stride 2 (the final store
+            # goes through the unpack kernel)
+            x = synth.fill(2 * (N // 2 + 1), 15, 1)
+            y = np.zeros(2 * N, np.float32)
+            plan = J.FFT(J.KIND_CROP, N, 1.0 / N)
+            bx, by = J.CBlock(x), J.RBlock(y)
+            vx, vy = bx.vview(0, 1, N // 2 + 1), by.vview(0, 2, N)
+            call = lambda: L.vsip_crfftop_f(plan.h, vx.h, vy.h)
+            nbytes, dt = 4 * N + 8 * (N // 2 + 1), "f32"
+            desc = f"vsip_crfftop_f {N // 2 + 1} c64 -> {N} f32 (real vector of stride 2), scale 1/{N}"
+        elif w == "vecrc":
             x = synth.fill(N, 8, 1)
             y = np.zeros(2 * (N // 2 + 1), np.float32)
             plan = J.FFT(J.KIND_RCOP, N, 1.0)
