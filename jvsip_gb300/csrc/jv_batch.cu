@@ -84,17 +84,19 @@ __device__ __forceinline__ void prefetch_l2_line(const void *p) {
 // point's row of transforms; other layouts are not prefetched.
 __device__ __forceinline__ void prefetch_tile(const TileDesc &d, int tid, int nthr) {
     const float2 *base = reinterpret_cast<const float2 *>(d.in) + (d.in_off + d.v0 * d.in_vs);
+    // every address is an element of the tile (the last line of a segment
+    // is taken at its last element)
     if (d.in_es == 1) {
         const int L = (d.N + 15) >> 4, tot = L * d.nt;
         for (int i = tid; i < tot; i += nthr) {
             const int v = i / L, l = i - v * L;
-            prefetch_l2_line(base + (long)v * d.in_vs + 16 * l);
+            prefetch_l2_line(base + (long)v * d.in_vs + min(16 * l, d.N - 1));
         }
     } else if (d.in_vs == 1) {
         const int L = (d.nt + 15) >> 4, tot = L * d.N;
         for (int i = tid; i < tot; i += nthr) {
             const int n = i / L, l = i - n * L;
-            prefetch_l2_line(base + (long)n * d.in_es + 16 * l);
+            prefetch_l2_line(base + (long)n * d.in_es + min(16 * l, d.nt - 1));
         }
     }
 }

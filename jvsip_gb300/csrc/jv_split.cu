@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(SQ_THREADS, 1) k_split1024(const SplitArgs a) 
     const uint32_t lane_addr = tmem + ((uint32_t)(r * 32) << 16);
     const uint32_t idesc1 = tc::idesc_f16(SPM, SPNN, BF ? 1 : 0);
     const uint32_t idesc2 = idesc1 | (1u << 15);  // A MN-major
-    const int ngroups = (int)((a.nvec + 3) / 4);  // nvec < 2^31 (checked by the launcher)
+    const int ngroups = (int)((a.nvec + 3) / 4);  // nvec <= 2^31 (checked by the launcher)
     const int gstep = (int)gridDim.x * SQG;
     const float s2 = BF ? 1.f : 0.0625f;  // folded into a.tw
     uint32_t pending = 2u;  // parity of a committed MMA phase this thread has not seen complete (2: none)
@@ -432,7 +432,8 @@ static bool split_tables() {
 // the call does not qualify and the plain kernels should run instead
 bool launch_split_f32(const Job &j, cudaStream_t st) {
     if (j.form != JVSIP_FORM_SPLIT_BF16 && j.form != JVSIP_FORM_SPLIT_FP16) return false;
-    if (j.kind != K_C2C || j.prec != P_F32 || j.N != SPN || j.nvec <= 0) return false;
+    // the kernel counts groups of 4 rows in 32-bit integers
+    if (j.kind != K_C2C || j.prec != P_F32 || j.N != SPN || j.nvec <= 0 || j.nvec > (1L << 31)) return false;
     const CView &ci = j.cin, &co = j.cout;
     if (ci.cst != 2 || co.cst != 2 || ci.es != 1 || co.es != 1) return false;
     if ((const float *)ci.im != (const float *)ci.re + 1 || (const float *)co.im != (const float *)co.re + 1) return false;
