@@ -5,12 +5,13 @@
 // four-step  Z[b][c] = sum_a X[a][b] w32^(ac),  Z'[b][c] = Z[b][c] w1024^(bc),
 // X[c + 32d] = sum_b Z'[b][c] w32^(bd).  Each step is a real GEMM whose A
 // operand is 128 x 128 (4 rows x 32 vectors; K = {hi, lo} x {re, im} x 32)
-// and whose B operand is 64 x 128 (the 32-point DFT matrix in the 2x2 real
-// form of complex multiplication, K = {W_hi, W_lo} x {re, im} x 32).  Three
-// products accumulate into one FP32 tensor-memory tile:
-//     X_hi * W_hi  +  X_lo * W_hi  +  X_hi * W_lo
-// (A K-blocks 0-3 with B 0-3, A 4-7 with B 0-3, A 0-3 with B 4-7), which
-// recovers about 22 (FP16) or 16 (BF16) significant bits of each operand.
+// and whose B operand is 128 x 128: the 32-point DFT matrix in the 2x2 real
+// form of complex multiplication, rounded to 16 bits (W_hi, N rows 0-63) and
+// its remainder rounded (W_lo, rows 64-127), each repeated for the hi and lo
+// halves of K.  Eight MMAs of K = 16 accumulate the FP32 tile
+//     columns 0-63:   (X_hi + X_lo) W_hi,   columns 64-127: (X_hi + X_lo) W_lo
+// whose two halves summed give all four hi/lo products, which recovers about
+// 22 (FP16) or 16 (BF16) significant bits of each operand.
 // FP16 operands are scaled per row by a power of two before step 1 (the row's
 // largest component into [2^13, 2^14)) and by the fixed 2^-4 before step 2
 // (|Z'| <= 32 sqrt(2) 2^14, so the scaled values stay below FP16's maximum);
@@ -20,9 +21,9 @@
 //
 // The kernel is persistent: one 1024-thread CTA per SM holding four
 // independent row groups (8 warps each: warp q takes row q % 4 of the group
-// and the half q / 4 of its vectors or outputs), one 32 KB A operand and 64
+// and the half q / 4 of its vectors or outputs), one 32 KB A operand and 128
 // tensor-memory columns per group, and one B operand and the [c][b] twiddle
-// table for the CTA (16 + 8 KB, bulk copies at the start).  A group loops over
+// table for the CTA (32 + 8 KB, bulk copies at the start).  A group loops over
 // groups of 4 rows; rows are read from and written to global memory directly
 // by coalesced per-lane accesses (lane = vector b on the way in, output c on
 // the way out), and the group's next rows are prefetched into L2 at the start
@@ -31,7 +32,7 @@
 // 1's operand is K-major (a lane writes 16-byte chunks of 8 consecutive a);
 // step 2's is MN-major (a lane holds Z'[b][c] for 16 consecutive c, written
 // as 16-byte chunks of 8 consecutive c), so no lane exchanges are needed.
-// One elected thread per group issues the 12 tcgen05.mma of a step and
+// One elected thread per group issues the 8 tcgen05.mma of a step and
 // commits them to the group's mbarrier; the group's warps synchronise on a
 // named barrier.  Every wait is bounded; on expiry the kernel records a
 // status that the next synchronisation reports (E_DEVICE), waits (bounded)
@@ -54,16 +55,16 @@ namespace jv {
 
 constexpr int SPN = 1024;                        // transform length of the form
 constexpr int SPM = 128;                         // GEMM M: 4 rows x 32
-constexpr int SPNN = 64;                         // GEMM N: {re, im} x 32
+constexpr int SPNN = 128;                        // GEMM N: {W_hi, W_lo} x {re, im} x 32
 constexpr uint32_t SP_B_LBO = (SPNN / 8) * 128;  // B: bytes between K-adjacent core matrices
-constexpr int SP_B_BYTES = 16 * SP_B_LBO;        // 16384
+constexpr int SP_B_BYTES = 16 * SP_B_LBO;        // 32768
 constexpr uint32_t SQ_KS = 128;                  // A: bytes between K-adjacent core matrices
 constexpr uint32_t SQ_MS = 2048;                 // A: bytes between M-adjacent core matrices
 constexpr int SQ_A_BYTES = 16 * SQ_MS;           // 32768 per group
 constexpr int SQG = 4;                           // row groups per CTA
 constexpr int SQW = 8;                           // warps per row group
 constexpr int SQ_THREADS = SQG * SQW * 32;       // 1024
-constexpr int SQ_TMEM_COLS = SQG * SPNN;         // 256
+constexpr int SQ_TMEM_COLS = SQG * SPNN;         // 512
 constexpr int SQ_TW_BYTES = 32 * 32 * 8;         // the [c][b] twiddle table
 constexpr uint32_t SP_WAIT_LIMIT = 1u << 24;
 
@@ -162,15 +163,32 @@ __device__ __forceinline__ void sts128(unsigned char *p, uint32_t x, uint32_t y,
     *reinterpret_cast<uint4 *>(p) = make_uint4(x, y, z, w);
 }
 
-// the three products of one step into tensor memory at `d`; da / db are the
-// descriptors of the operands' first K chunks (a chunk of 16 k is 2 * SQ_KS
-// bytes further in A and 2 * SP_B_LBO in B: the address field counts 16 bytes)
+// one step into tensor memory at `d`: the 8 K-chunks of 16 (X_hi then X_lo,
+// each {re, im} x 32) against B, whose N = 128 columns are W_hi and W_lo side
+// by side (the same for both halves of K), so columns 0-63 accumulate
+// (X_hi + X_lo) W_hi and columns 64-127 (X_hi + X_lo) W_lo -- all four hi/lo
+// products.  da / db are the descriptors of the operands' first K chunks (a
+// chunk is 2 * SQ_KS bytes further in A and 2 * SP_B_LBO in B; the address
+// field counts 16 bytes)
 __device__ __forceinline__ void split_mma(uint32_t d, uint64_t da, uint64_t db, uint32_t idesc) {
 #pragma unroll
-    for (int i = 0; i < 12; i++) {
-        const int ka = (i < 8) ? i : i - 8;  // A K-chunk: hi 0-3, lo 4-7, hi 0-3
-        const int kb = (i < 4) ? i : i - 4;  // B K-chunk: W_hi 0-3, W_hi 0-3, W_lo 4-7
-        tc::mma_f16(d, da + (uint64_t)(ka * 2 * SQ_KS / 16), db + (uint64_t)(kb * 2 * SP_B_LBO / 16), idesc, i > 0);
+    for (int k = 0; k < 8; k++)
+        tc::mma_f16(d, da + (uint64_t)(k * 2 * SQ_KS / 16), db + (uint64_t)(k * 2 * SP_B_LBO / 16), idesc, k > 0);
+}
+
+// the step's result for 8 columns (c or d) from j0 of this lane's row: the
+// sum of the W_hi and W_lo halves of the tile
+__device__ __forceinline__ void tile_read8(uint32_t lane_addr, int j0, float (&re)[8], float (&im)[8]) {
+    float a[8], b[8];
+    tc::tmem_ld8(lane_addr + j0, re);
+    tc::tmem_ld8(lane_addr + 64 + j0, a);
+    tc::tmem_ld8(lane_addr + 32 + j0, im);
+    tc::tmem_ld8(lane_addr + 96 + j0, b);
+    tc::tmem_ld_wait();
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        re[i] += a[i];
+        im[i] += b[i];
     }
 }
 
@@ -284,9 +302,7 @@ __global__ void __launch_bounds__(SQ_THREADS, 1) k_split1024(const SplitArgs a) 
         for (int j = 0; j < 2; j++) {
             float zr[8], zi[8];
             if (ok) {
-                tc::tmem_ld8(lane_addr + 16 * h + 8 * j, zr);
-                tc::tmem_ld8(lane_addr + 32 + 16 * h + 8 * j, zi);
-                tc::tmem_ld_wait();
+                tile_read8(lane_addr, 16 * h + 8 * j, zr, zi);
             } else {
 #pragma unroll
                 for (int i = 0; i < 8; i++) zr[i] = zi[i] = 0.f;
@@ -331,17 +347,15 @@ __global__ void __launch_bounds__(SQ_THREADS, 1) k_split1024(const SplitArgs a) 
             const bool live = row < a.nvec;
             float2 *dst = a.out + a.off_out + (live ? row : 0) * a.vs_out + 512 * h + lane;
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                float yr[4], yi[4];
-                tc::tmem_ld4(lane_addr + 16 * h + 4 * j, yr);
-                tc::tmem_ld4(lane_addr + 32 + 16 * h + 4 * j, yi);
-                tc::tmem_ld_wait();
+            for (int j = 0; j < 2; j++) {
+                float yr[8], yi[8];
+                tile_read8(lane_addr, 16 * h + 8 * j, yr, yi);
                 if (live) {
 #pragma unroll
-                    for (int i = 0; i < 4; i++) {
+                    for (int i = 0; i < 8; i++) {
                         float2 o = make_float2(yr[i] * f, yi[i] * f);
                         if (a.inv) o.y = -o.y;
-                        dst[32 * (4 * j + i)] = o;
+                        dst[32 * (8 * j + i)] = o;
                     }
                 }
             }
@@ -363,11 +377,12 @@ __global__ void __launch_bounds__(SQ_THREADS, 1) k_split1024(const SplitArgs a) 
 }
 
 // ---------------------------------------------------------------- host side
-// B operand of both steps: row n = ro*32 + c, column k = part*64 + ri*32 + a,
-// the real 2x2 form of w32^(ac) = exp(-2 pi i ac/32) (FP64, then split):
-// (ro, ri) = (re, re): cos, (re, im): -sin, (im, re): +sin, (im, im): cos;
-// part 0 holds the 16-bit rounding W_hi of each entry, part 1 the rounding
-// W_lo of its remainder.
+// B operand of both steps: row n = pw*64 + ro*32 + c, column k = px*64 +
+// ri*32 + a, the real 2x2 form of w32^(ac) = exp(-2 pi i ac/32) (FP64, then
+// split): (ro, ri) = (re, re): cos, (re, im): -sin, (im, re): +sin, (im, im):
+// cos; rows pw = 0 hold the 16-bit rounding W_hi of each entry, rows pw = 1
+// the rounding W_lo of its remainder, the same for both halves px of K (the
+// hi and lo parts of the data).
 template <bool BF>
 static std::vector<uint16_t> b_operand() {
     std::vector<uint16_t> b(SP_B_BYTES / 2, 0);
@@ -392,8 +407,10 @@ static std::vector<uint16_t> b_operand() {
                         lo = __half_as_ushort(__float2half_rn((float)(val - (double)__half2float(h))));
                     }
                     const int n = ro * 32 + c;
-                    b[core_off(n, 0 * 64 + ri * 32 + aa, SP_B_LBO) / 2] = hi;
-                    b[core_off(n, 1 * 64 + ri * 32 + aa, SP_B_LBO) / 2] = lo;
+                    for (int px = 0; px < 2; px++) {
+                        b[core_off(n, px * 64 + ri * 32 + aa, SP_B_LBO) / 2] = hi;
+                        b[core_off(64 + n, px * 64 + ri * 32 + aa, SP_B_LBO) / 2] = lo;
+                    }
                 }
     return b;
 }
@@ -458,11 +475,13 @@ bool launch_split_f32(const Job &j, cudaStream_t st) {
     a.bop = (const uint4 *)g_bop[bf ? 1 : 0];
     a.tw = (const float2 *)g_tw[bf ? 1 : 0];
     a.status = g_status;
-    // operand reads: A chunks start at 2 * ka * SQ_KS (ka < 8) and span 16
+    // operand reads: A chunks start at 2 * k * SQ_KS (k < 8) and span 16
     // core matrices along m (SQ_MS apart) and 2 along k, ending at byte
     // 14 * SQ_KS + 15 * SQ_MS + 2 * SQ_KS - 1 < SQ_A_BYTES of the group's A
     // (whichever of the two descriptor strides is taken along m); B chunks
-    // end at byte 16 * SP_B_LBO - 1 of B: all inside the operands
+    // start at 2 * k * SP_B_LBO and span 16 core matrices along n (128 apart)
+    // and 2 along k, ending at byte 16 * SP_B_LBO - 1 of B: all inside the
+    // operands
     const long ngroups = (j.nvec + 3) / 4;
     Device *d = device();
     long grid = (ngroups + SQG - 1) / SQG;

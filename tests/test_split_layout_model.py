@@ -40,7 +40,7 @@ def all_elements():
 
 
 def test_layout_constants():
-    assert CONSTS["SPM"] == 128 and CONSTS["SPNN"] == 64 and A_BYTES == 16 * MS
+    assert CONSTS["SPM"] == 128 and A_BYTES == 16 * MS
     assert CONSTS["SQ_THREADS"] == CONSTS["SQG"] * CONSTS["SQW"] * 32 == 1024
     assert "a_off_k(m, ka)" in SRC and "a_off_mn(mc, lane)" in SRC
     # both layouts address the same 32 KB: (m, k) -> distinct bytes
@@ -99,9 +99,9 @@ def test_mma_reads_inside_a_either_stride_reading():
         for s_m, s_k in ((MS, KS), (KS, MS)):
             last = start + 15 * s_m + 1 * s_k + 127  # 16 core matrices along m, 2 along k
             assert last < A_BYTES
-    for i in range(12):
-        kb = i if i < 4 else i - 4
-        assert kb * 2 * CONSTS["SP_B_LBO"] + CONSTS["SP_B_LBO"] + 8 * 128 <= CONSTS["SP_B_BYTES"]
+    assert CONSTS["SPNN"] == 128 and CONSTS["SP_B_BYTES"] == 16 * CONSTS["SP_B_LBO"]
+    for k in range(8):  # B chunks: 16 core matrices along n (128 B apart), 2 along k
+        assert k * 2 * CONSTS["SP_B_LBO"] + CONSTS["SP_B_LBO"] + 16 * 128 <= CONSTS["SP_B_BYTES"]
 
 
 def test_cta_shared_memory_fits():
