@@ -205,9 +205,10 @@ __device__ __forceinline__ void load_half(const SplitArgs &a, long row, int h, i
     }
 }
 
-// Persistent kernel: gridDim.x CTAs of SQG row groups; group slot s of CTA
-// blk processes the 4-row groups g = blk * SQG + s, stepping by gridDim.x * SQG.
-// The slot's next rows are prefetched into L2 at the start of each iteration.
+// Persistent kernel: gridDim.x CTAs of SQG row groups; group slot grp of CTA
+// blk processes the 4-row groups g = grp * gridDim.x + blk, stepping by
+// gridDim.x * SQG.  The slot's next rows are prefetched into L2 at the start
+// of each iteration.
 template <bool BF>
 __global__ void __launch_bounds__(SQ_THREADS, 1) k_split1024(const SplitArgs a) {
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -235,7 +236,9 @@ __global__ void __launch_bounds__(SQ_THREADS, 1) k_split1024(const SplitArgs a) 
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    bool ok = tc::mbar_wait(&bbar, 0, SP_WAIT_LIMIT);
+    // the B operand and twiddle copies are waited for after the first rows'
+    // loads are issued, so the two overlap
+    bool ok = true, b_waited = false;
     const uint32_t tmem = tslot + (uint32_t)(grp * SPNN);
     // this warp's tensor-memory lanes: rows 32r..32r+31 of the group's tile
     const uint32_t lane_addr = tmem + ((uint32_t)(r * 32) << 16);
@@ -245,10 +248,12 @@ __global__ void __launch_bounds__(SQ_THREADS, 1) k_split1024(const SplitArgs a) 
     const int gstep = (int)gridDim.x * SQG;
     const float s2 = BF ? 1.f : 0.0625f;  // folded into a.tw
     uint32_t pending = 2u;  // parity of a committed MMA phase this thread has not seen complete (2: none)
-    for (int g = (int)blockIdx.x * SQG + grp; g < ngroups; g += gstep) {
+    // slot s = grp * gridDim.x + blockIdx.x takes the groups s, s + gstep, ...:
+    // the last, partial round of groups spreads over all CTAs
+    for (int g = grp * (int)gridDim.x + (int)blockIdx.x; g < ngroups; g += gstep) {
         const long row = (long)g * 4 + r;
         {
-            // the slot's group after next into L2: 4 rows x 64 lines of 128 bytes
+            // the slot's next group into L2: 4 rows x 64 lines of 128 bytes
             const long rn = ((long)g + gstep) * 4 + (gt >> 6);
             if (rn < a.nvec) prefetch_l2(a.in + a.off_in + rn * a.vs_in + (gt & 63) * 16);
         }
@@ -260,6 +265,10 @@ __global__ void __launch_bounds__(SQ_THREADS, 1) k_split1024(const SplitArgs a) 
             for (int i = 0; i < 16; i++) mx = fmaxf(mx, fmaxf(fabsf(v[i].x), fabsf(v[i].y)));
             mx = warp_max(mx);
             if (lane == 0) smax[grp][q] = mx;
+        }
+        if (!b_waited) {
+            ok = tc::mbar_wait(&bbar, 0, SP_WAIT_LIMIT) && ok;
+            b_waited = true;
         }
         ok = bar_and(bar_id, bar_n, ok);
         if (!ok) break;
@@ -364,6 +373,9 @@ __global__ void __launch_bounds__(SQ_THREADS, 1) k_split1024(const SplitArgs a) 
         // before the next products overwrite the tile
         tc::fence_before_sync();
     }
+    // a slot without groups still waits for the B and twiddle copies into the
+    // CTA's shared memory before the CTA can end
+    if (!b_waited) ok = tc::mbar_wait(&bbar, 0, SP_WAIT_LIMIT) && ok;
     if (!ok) {
         atomicExch(a.status, 1);
         // let MMAs and the B copy still in flight finish (bounded) before the
