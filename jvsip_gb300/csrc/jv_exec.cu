@@ -457,6 +457,48 @@ static bool real_as_complex(const RView &r, long nvec, size_t esz, CView *c) {
 // scratch, steps into the real output as complex pairs, or into scratch and
 // the final store).  Returns with *handled unset when the call does not
 // qualify (the multi-pass global path takes it).
+// Bytes of scratch a long call needs: its data once for the two steps of a
+// c2c call of several vectors, twice otherwise (the single-vector passes and
+// C2R use two halves).
+static size_t long_scratch_need(const Job &j) {
+    const size_t esz = j.prec == P_F32 ? sizeof(float) : sizeof(double);
+    const size_t one = (size_t)j.nvec * j.N * 2 * esz;
+    return (j.kind == K_C2C && j.nvec > 1) ? one : 2 * one;
+}
+
+// The plan's scratch of at least `need` bytes (held by the plan: a captured
+// call replays into it).  quiet: a failed allocation records no error (the
+// caller has another path).
+static bool long_scratch(LongPlan *lp, size_t need, bool quiet) {
+    if (lp->scratch_bytes >= need) return true;
+    const int err0 = jvsip_gpu_last_error();
+    dfree(lp->scratch);
+    lp->scratch = dmalloc(need);
+    lp->scratch_bytes = lp->scratch ? need : 0;
+    if (lp->scratch) return true;
+    if (quiet) {
+        if (err0 == 0 && jvsip_gpu_last_error() != 0) jvsip_gpu_clear_error();
+    } else if (!jvsip_gpu_last_error()) {
+        set_error(E_ALLOC, "scratch of a long transform");
+    }
+    return false;
+}
+
+// few transforms of a length with a decomposition: two steps over many CTAs
+// instead of one CTA per transform
+static bool long_few(const Job &j) {
+    return j.lp && j.nvec * 2 < (long)device()->sms && j.N >= kLongFewMin;
+}
+// single-precision c2c columns (adjacent vectors on both sides) of a length
+// with a decomposition: two steps whatever their count.  Measured on columns of
+// 8192-16384 points, 64-2048 of them, against the shared-memory kernel's
+// column tiles: 1.0-2.0x (16384 x 1024: 1799 against 1013 GB/s; 10000 x 1024:
+// 1848 against 917; 8192 x 2048: 1806 against 1436).
+static bool long_columns(const Job &j) {
+    return j.lp && j.kind == K_C2C && j.prec == P_F32 && j.nvec > 1 && j.N >= kLongFewMin && labs(j.cin.vs) == 1 &&
+           labs(j.cout.vs) == 1;
+}
+
 static bool run_long(Job &j, cudaStream_t st, bool *handled) {
     *handled = false;
     LongPlan *lp = j.lp;
@@ -473,21 +515,11 @@ static bool run_long(Job &j, cudaStream_t st, bool *handled) {
     // in the two steps, 815 in two passes; 2^26 points 715 against 891)
     const bool sp = !lp->sp_radix.empty() && nv == 1 && j.prec == P_F32 && j.cout.es == 1 &&
                     ((j.kind == K_C2C && j.cin.es == 1) || (j.kind == K_R2C && lp->sp_radix.size() >= 3));
-    // the scratch is sized once for every path of the plan (twice the data:
-    // the passes and C2R use two halves): a captured call's graph holds its
-    // address, so it is never reallocated while the plan lives
-    const size_t need = 2 * one;
+    // the plan's call shape is fixed, so the scratch is sized once: a captured
+    // call's graph holds its address, and it is never reallocated while the
+    // plan lives
     *handled = true;
-    if (lp->scratch_bytes < need) {
-        // held by the plan (a captured call replays into it)
-        dfree(lp->scratch);
-        lp->scratch = dmalloc(need);
-        lp->scratch_bytes = lp->scratch ? need : 0;
-        if (!lp->scratch) {
-            if (!jvsip_gpu_last_error()) set_error(E_ALLOC, "scratch of a long transform");
-            return false;
-        }
-    }
+    if (!long_scratch(lp, long_scratch_need(j), false)) return false;
     char *sc = (char *)lp->scratch;
     if (sp && j.kind == K_C2C) return sp_passes(j, lp, j.cin, j.cout, j.inv, j.has_scale, j.scale, sc, esz, st);
     if (j.kind == K_C2C)
@@ -529,10 +561,10 @@ static bool run_job(Job &j, cudaStream_t st) {
     if (j.form == JVSIP_FORM_DF64 && j.twdd) {
         if (launch_fast_dd(j, st)) return jvsip_gpu_last_error() == 0;
     }
-    // few transforms of a length with a decomposition: two steps over many
-    // CTAs instead of one CTA per transform
-    const bool few = j.lp && j.nvec * 2 < (long)device()->sms && j.N >= kLongFewMin;
-    if (job_in_smem(j) && !few) {
+    // columns take the two steps when the plan's scratch can be had, the
+    // tile kernels otherwise
+    const bool two = long_few(j) || (long_columns(j) && long_scratch(j.lp, long_scratch_need(j), true));
+    if (job_in_smem(j) && !two) {
         if (j.prec == P_F32) {
             if (launch_fast_f32(j, st)) return true;
             return launch_smem_f32(j, st);
@@ -580,11 +612,11 @@ static bool run_job_planned(Plan *p, Job &j, cudaStream_t st) {
     // a long transform captures once its plan holds the scratch for this call
     const size_t esz = j.prec == P_F32 ? sizeof(float) : sizeof(double);
     CView tmpv;
-    const bool long_job = j.lp && ((j.kind == K_C2C && interleaved(j.cin, esz) && interleaved(j.cout, esz)) ||
-                                   (j.kind == K_R2C && interleaved(j.cout, esz) &&
-                                    real_as_complex(j.rin, j.nvec, esz, &tmpv)) ||
-                                   j.kind == K_C2R);
-    const bool long_ready = long_job && j.lp->scratch_bytes >= (size_t)j.nvec * j.N * 2 * esz * 2;
+    const bool long_job = j.lp && (!job_in_smem(j) || long_few(j) || long_columns(j)) &&
+                          ((j.kind == K_C2C && interleaved(j.cin, esz) && interleaved(j.cout, esz)) ||
+                           (j.kind == K_R2C && interleaved(j.cout, esz) && real_as_complex(j.rin, j.nvec, esz, &tmpv)) ||
+                           j.kind == K_C2R);
+    const bool long_ready = long_job && j.lp->scratch_bytes >= long_scratch_need(j);
     if (!split && !job_in_smem(j) && !long_job) return run_job(j, st);
     CallGraph *e = nullptr;
     for (CallGraph &g : p->graphs)

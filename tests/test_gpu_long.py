@@ -275,3 +275,80 @@ def test_long_plan_scratch_stays_put_across_paths():
         v.destroy()
     for b in (b2, b1, c2, c1):
         b.destroy()
+
+
+@pytest.mark.parametrize("N,M,d,inplace", [(8192, 200, J.VSIP_FFT_FWD, False), (10000, 160, J.VSIP_FFT_INV, True),
+                                           (16384, 96, J.VSIP_FFT_FWD, True), (13824, 77, J.VSIP_FFT_INV, False)])
+def test_long_columns_many(N, M, d, inplace):
+    """Single-precision c2c columns of 8192+ points that one CTA takes run as
+    the two steps whatever their count (two launches, the plan's scratch):
+    forward and inverse with scale 1/N, in place and out of place; the same
+    plan on a column-major matrix (vectors not adjacent) runs the column
+    kernel (one launch)."""
+    L = J.lib()
+    z = rnd(N * M, N + M).reshape(N, M)
+    scale = 1.0 if d == J.VSIP_FFT_FWD else 1.0 / N
+    ref = np.fft.fft(z, axis=0) if d == J.VSIP_FFT_FWD else np.fft.ifft(z, axis=0)
+    x = interleave(z, np.float32)
+    y = x if inplace else np.zeros_like(x)
+    bx = J.CBlock(x)
+    bx.admit(True)
+    by = bx if inplace else J.CBlock(y)
+    if not inplace:
+        by.admit(False)
+    vx, vy = bx.view(0, M, N, 1, M), by.view(0, M, N, 1, M)
+    p = J.FFTM(J.KIND_CCIP if inplace else J.KIND_CCOP, N, M, scale, d, J.VSIP_COL, ntimes=1)
+    n0 = L.jvsip_gpu_kernel_launches()
+    if inplace:
+        p.ccfftmip(vx)
+    else:
+        p.ccfftmop(vx, vy)
+    assert L.jvsip_gpu_synchronize() == 0, J.last_error()
+    assert L.jvsip_gpu_kernel_launches() - n0 == 2
+    by.sync()
+    assert rel(cplx(y).reshape(N, M), ref) <= tol(N, np.float32)
+    # column-major storage: vector v at v * N, element n at n (not adjacent)
+    xc = interleave(z.T.copy(), np.float32)
+    yc = np.zeros_like(xc)
+    cx, cy = J.CBlock(xc), J.CBlock(yc)
+    cx.admit(True)
+    cy.admit(False)
+    ux, uy = cx.view(0, 1, N, N, M), cy.view(0, 1, N, N, M)
+    q = J.FFTM(J.KIND_CCOP, N, M, scale, d, J.VSIP_COL, ntimes=1)
+    n0 = L.jvsip_gpu_kernel_launches()
+    q.ccfftmop(ux, uy)
+    assert L.jvsip_gpu_synchronize() == 0, J.last_error()
+    assert L.jvsip_gpu_kernel_launches() - n0 == 1
+    cy.sync()
+    assert rel(cplx(yc).reshape(M, N).T, ref) <= tol(N, np.float32)
+    for v in (vx, vy, ux, uy) if not inplace else (vx, ux, uy):
+        v.destroy()
+    for b in (bx, by, cx, cy) if not inplace else (bx, cx, cy):
+        b.destroy()
+
+
+def test_long_columns_many_graph_replay():
+    """A column plan created with ntimes == 0 captures the two steps once its
+    scratch exists and replays them with the direct call's results."""
+    N, M = 16384, 128
+    z = rnd(N * M, 29).reshape(N, M)
+    x = interleave(z, np.float32)
+    y1, y2 = np.zeros_like(x), np.zeros_like(x)
+    bx, b1, b2 = J.CBlock(x), J.CBlock(y1), J.CBlock(y2)
+    for b in (bx, b1, b2):
+        b.admit(True)
+    many = J.FFTM(J.KIND_CCOP, N, M, 1.0, J.VSIP_FFT_FWD, J.VSIP_COL, ntimes=0)
+    once = J.FFTM(J.KIND_CCOP, N, M, 1.0, J.VSIP_FFT_FWD, J.VSIP_COL, ntimes=1)
+    vx, v1, v2 = bx.view(0, M, N, 1, M), b1.view(0, M, N, 1, M), b2.view(0, M, N, 1, M)
+    for _ in range(4):
+        many.ccfftmop(vx, v1)
+        once.ccfftmop(vx, v2)
+    assert int(J.lib().jvsip_fftm_graphs(many.h)) == 1
+    b1.sync()
+    b2.sync()
+    assert np.array_equal(y1, y2)
+    assert rel(cplx(y1).reshape(N, M), np.fft.fft(z, axis=0)) <= tol(N, np.float32)
+    for v in (vx, v1, v2):
+        v.destroy()
+    for b in (bx, b1, b2):
+        b.destroy()
