@@ -490,13 +490,15 @@ static bool long_few(const Job &j) {
     return j.lp && j.nvec * 2 < (long)device()->sms && j.N >= kLongFewMin;
 }
 // single-precision c2c columns (adjacent vectors on both sides) of a length
-// with a decomposition: two steps whatever their count.  Measured on columns of
-// 8192-16384 points, 64-2048 of them, against the shared-memory kernel's
-// column tiles: 1.0-2.0x (16384 x 1024: 1799 against 1013 GB/s; 10000 x 1024:
-// 1848 against 917; 8192 x 2048: 1806 against 1436).
+// with a decomposition from kColStepsMin points, not taken by the
+// register-resident column tiles: two steps whatever their count.  Measured
+// against the shared-memory kernel's column tiles: 16384 x 1024: 1799 against
+// 1013 GB/s; 10000 x 1024: 1848 against 917; 8192 x 2048: 1806 against 1436;
+// 7000 x 512: 1319 against 782; 3000 x 1024: 1164 against 874 (and slower than
+// the register-resident tiles: 4096 x 1024: 1457 against 2283).
 static bool long_columns(const Job &j) {
-    return j.lp && j.kind == K_C2C && j.prec == P_F32 && j.nvec > 1 && j.N >= kLongFewMin && labs(j.cin.vs) == 1 &&
-           labs(j.cout.vs) == 1;
+    return j.lp && j.kind == K_C2C && j.prec == P_F32 && j.nvec > 1 && j.N >= kColStepsMin && !fast_step_len(j.N) &&
+           labs(j.cin.vs) == 1 && labs(j.cout.vs) == 1;
 }
 
 static bool run_long(Job &j, cudaStream_t st, bool *handled) {

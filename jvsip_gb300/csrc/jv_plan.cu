@@ -440,11 +440,12 @@ static bool build_long(Plan *p) {
     const long lim = smem_max_len(p->prec, K_C2C);
     // lengths one CTA takes get the decomposition too when the plan has few
     // transforms (one CTA per transform would leave most SMs idle), and
-    // single-precision c2c column plans of 8192 points or more (their adjacent
-    // columns run as two steps, faster than the column tiles)
+    // single-precision c2c column plans from kColStepsMin points that the
+    // register-resident column tiles do not take (their adjacent columns run
+    // as two steps, faster than the shared-memory kernel's column tiles)
     const bool few = p->mN * 2 < (long)device()->sms && N >= kLongFewMin;
     const bool cols = p->major == 1 && p->prec == P_F32 && (p->type == JV_CCFFTOP || p->type == JV_CCFFTIP) &&
-                      N >= kLongFewMin;
+                      N >= kColStepsMin && !fast_step_len(N);
     if ((N <= lim && !few && !cols) || N >= (1L << 31)) return true;
     const long maxt = p->prec == P_F32 ? 1024 : 512;
     long best = 0;

@@ -269,9 +269,9 @@ int jvsip_fftm_autotune_plain_f(size_t n, const unsigned long *lengths, int cls)
     for (size_t i = 0; i < n && rc == 0; i++) {
         const long N = (long)lengths[i];
         if (N < 2 || N > 16384) continue;
-        // adjacent columns of kLongFewMin points or more run as the two steps,
-        // never on the tiles searched here
-        if (cls && N >= kLongFewMin) continue;
+        // adjacent columns that run as the two steps never use the tiles
+        // searched here
+        if (cls && N >= kColStepsMin && !fast_step_len(N)) continue;
         const std::vector<std::vector<int>> scheds = schedule_candidates(N, 1024, 6);
         if (scheds.empty()) continue;
         const long cnt = std::max(8L, (32L << 20) / (16 * N));

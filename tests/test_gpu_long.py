@@ -278,13 +278,15 @@ def test_long_plan_scratch_stays_put_across_paths():
 
 
 @pytest.mark.parametrize("N,M,d,inplace", [(8192, 200, J.VSIP_FFT_FWD, False), (10000, 160, J.VSIP_FFT_INV, True),
-                                           (16384, 96, J.VSIP_FFT_FWD, True), (13824, 77, J.VSIP_FFT_INV, False)])
+                                           (16384, 96, J.VSIP_FFT_FWD, True), (13824, 77, J.VSIP_FFT_INV, False),
+                                           (3000, 200, J.VSIP_FFT_FWD, False), (6000, 90, J.VSIP_FFT_INV, True),
+                                           (3125, 130, J.VSIP_FFT_INV, False)])
 def test_long_columns_many(N, M, d, inplace):
-    """Single-precision c2c columns of 8192+ points that one CTA takes run as
-    the two steps whatever their count (two launches, the plan's scratch):
-    forward and inverse with scale 1/N, in place and out of place; the same
-    plan on a column-major matrix (vectors not adjacent) runs the column
-    kernel (one launch)."""
+    """Single-precision c2c columns from 3000 points that one CTA takes and the
+    register-resident column tiles do not run as the two steps whatever their
+    count (two launches, the plan's scratch): forward and inverse with scale
+    1/N, in place and out of place; the same plan on a column-major matrix
+    (vectors not adjacent) runs the column kernel (one launch)."""
     L = J.lib()
     z = rnd(N * M, N + M).reshape(N, M)
     scale = 1.0 if d == J.VSIP_FFT_FWD else 1.0 / N
@@ -351,4 +353,30 @@ def test_long_columns_many_graph_replay():
     for v in (vx, v1, v2):
         v.destroy()
     for b in (bx, b1, b2):
+        b.destroy()
+
+
+@pytest.mark.parametrize("N", [2048, 2400, 4096])
+def test_columns_of_register_resident_lengths_stay_one_launch(N):
+    """Column lengths the register-resident column tiles take, and lengths
+    below 3000 points, keep one column-tile launch whatever the column count."""
+    L = J.lib()
+    M = 200
+    z = rnd(N * M, N).reshape(N, M)
+    x = interleave(z, np.float32)
+    y = np.zeros_like(x)
+    bx, by = J.CBlock(x), J.CBlock(y)
+    bx.admit(True)
+    by.admit(False)
+    vx, vy = bx.view(0, M, N, 1, M), by.view(0, M, N, 1, M)
+    p = J.FFTM(J.KIND_CCOP, N, M, 1.0, J.VSIP_FFT_FWD, J.VSIP_COL, ntimes=1)
+    n0 = L.jvsip_gpu_kernel_launches()
+    p.ccfftmop(vx, vy)
+    assert L.jvsip_gpu_synchronize() == 0, J.last_error()
+    assert L.jvsip_gpu_kernel_launches() - n0 == 1
+    by.sync()
+    assert rel(cplx(y).reshape(N, M), np.fft.fft(z, axis=0)) <= tol(N, np.float32)
+    for v in (vx, vy):
+        v.destroy()
+    for b in (bx, by):
         b.destroy()
