@@ -285,6 +285,156 @@ template <typename C> struct Dft<C, 12> : DftPQ<C, 4, 3> {};
 template <typename C> struct Dft<C, 14> : DftPQ<C, 2, 7> {};
 template <typename C> struct Dft<C, 15> : DftPQ<C, 3, 5> {};
 
+// cos and sin of 2 pi i / R (i = 1 .. (R - 1) / 2) for the odd-prime codelets:
+// constants that the unrolled loops fold into their multiply-adds
+template <int R> __host__ __device__ constexpr double prime_cos(int i);
+template <int R> __host__ __device__ constexpr double prime_sin(int i);
+template <> __host__ __device__ constexpr double prime_cos<11>(int i) {
+    return i == 1 ? 0.8412535328311812
+         : i == 2 ? 0.41541501300188644
+         : i == 3 ? -0.142314838273285
+         : i == 4 ? -0.654860733945285
+         : -0.9594929736144974;
+}
+template <> __host__ __device__ constexpr double prime_sin<11>(int i) {
+    return i == 1 ? 0.5406408174555976
+         : i == 2 ? 0.9096319953545183
+         : i == 3 ? 0.9898214418809328
+         : i == 4 ? 0.7557495743542583
+         : 0.28173255684142967;
+}
+template <> __host__ __device__ constexpr double prime_cos<13>(int i) {
+    return i == 1 ? 0.8854560256532099
+         : i == 2 ? 0.5680647467311559
+         : i == 3 ? 0.120536680255323
+         : i == 4 ? -0.35460488704253545
+         : i == 5 ? -0.7485107481711012
+         : -0.970941817426052;
+}
+template <> __host__ __device__ constexpr double prime_sin<13>(int i) {
+    return i == 1 ? 0.4647231720437685
+         : i == 2 ? 0.8229838658936564
+         : i == 3 ? 0.992708874098054
+         : i == 4 ? 0.9350162426854148
+         : i == 5 ? 0.6631226582407952
+         : 0.23931566428755768;
+}
+template <> __host__ __device__ constexpr double prime_cos<17>(int i) {
+    return i == 1 ? 0.9324722294043558
+         : i == 2 ? 0.7390089172206591
+         : i == 3 ? 0.4457383557765383
+         : i == 4 ? 0.09226835946330202
+         : i == 5 ? -0.2736629900720829
+         : i == 6 ? -0.6026346363792563
+         : i == 7 ? -0.850217135729614
+         : -0.9829730996839018;
+}
+template <> __host__ __device__ constexpr double prime_sin<17>(int i) {
+    return i == 1 ? 0.3612416661871529
+         : i == 2 ? 0.6736956436465572
+         : i == 3 ? 0.8951632913550623
+         : i == 4 ? 0.9957341762950345
+         : i == 5 ? 0.961825643172819
+         : i == 6 ? 0.7980172272802396
+         : i == 7 ? 0.5264321628773561
+         : 0.18374951781657037;
+}
+template <> __host__ __device__ constexpr double prime_cos<19>(int i) {
+    return i == 1 ? 0.9458172417006346
+         : i == 2 ? 0.7891405093963936
+         : i == 3 ? 0.5469481581224269
+         : i == 4 ? 0.24548548714079924
+         : i == 5 ? -0.08257934547233227
+         : i == 6 ? -0.4016954246529694
+         : i == 7 ? -0.6772815716257409
+         : i == 8 ? -0.879473751206489
+         : -0.9863613034027223;
+}
+template <> __host__ __device__ constexpr double prime_sin<19>(int i) {
+    return i == 1 ? 0.32469946920468346
+         : i == 2 ? 0.6142127126896678
+         : i == 3 ? 0.8371664782625285
+         : i == 4 ? 0.9694002659393304
+         : i == 5 ? 0.9965844930066698
+         : i == 6 ? 0.9157733266550574
+         : i == 7 ? 0.7357239106731318
+         : i == 8 ? 0.4759473930370737
+         : 0.16459459028073403;
+}
+template <> __host__ __device__ constexpr double prime_cos<23>(int i) {
+    return i == 1 ? 0.9629172873477992
+         : i == 2 ? 0.8544194045464886
+         : i == 3 ? 0.6825531432186541
+         : i == 4 ? 0.4600650377311522
+         : i == 5 ? 0.20345601305263375
+         : i == 6 ? -0.06824241336467088
+         : i == 7 ? -0.33487961217098616
+         : i == 8 ? -0.5766803221148671
+         : i == 9 ? -0.7757112907044197
+         : i == 10 ? -0.917211301505453
+         : -0.9906859460363306;
+}
+template <> __host__ __device__ constexpr double prime_sin<23>(int i) {
+    return i == 1 ? 0.2697967711570243
+         : i == 2 ? 0.5195839500354336
+         : i == 3 ? 0.730835964278124
+         : i == 4 ? 0.8878852184023752
+         : i == 5 ? 0.9790840876823229
+         : i == 6 ? 0.9976687691905392
+         : i == 7 ? 0.9422609221188205
+         : i == 8 ? 0.8169698930104421
+         : i == 9 ? 0.631087944326053
+         : i == 10 ? 0.3984010898462414
+         : 0.1361666490962471;
+}
+
+// Odd prime R as a direct O(R^2) DFT in registers, halved by the symmetry of
+// the roots: with s_n = v_n + v_(R-n) and d_n = v_n - v_(R-n) (n = 1 .. H,
+// H = (R - 1) / 2), Y_0 = v_0 + sum s_n and, for k = 1 .. H,
+// Y_k = a_k - i b_k, Y_(R-k) = a_k + i b_k, a_k = v_0 + sum s_n cos(2 pi nk/R),
+// b_k = sum d_n sin(2 pi nk/R) -- the forward DFT of VI_dftm_f
+// (c_VSIP_src/VI_fftm_building_blocks_f.h:95-155) for one butterfly.
+template <typename C, int R> struct DftOdd {
+    static __device__ __forceinline__ void run(C *v) {
+        typedef decltype(C::x) T;
+        constexpr int H = (R - 1) / 2;
+        C s[H], d[H];
+        C y0 = v[0];
+#pragma unroll
+        for (int n = 1; n <= H; n++) {
+            s[n - 1] = cadd(v[n], v[R - n]);
+            d[n - 1] = csub(v[n], v[R - n]);
+            y0 = cadd(y0, s[n - 1]);
+        }
+        C y[R];
+        y[0] = y0;
+#pragma unroll
+        for (int k = 1; k <= H; k++) {
+            C a = v[0], b = mk<C>((T)0, (T)0);
+#pragma unroll
+            for (int n = 1; n <= H; n++) {
+                // 2 pi nk/R reduced to i = nk mod R, folded into 1 .. H (sin changes sign)
+                const int e = (n * k) % R;
+                const int i = e <= H ? e : R - e;
+                const T c = (T)prime_cos<R>(i), sn = (T)(e <= H ? prime_sin<R>(i) : -prime_sin<R>(i));
+                a.x += s[n - 1].x * c;
+                a.y += s[n - 1].y * c;
+                b.x += d[n - 1].x * sn;
+                b.y += d[n - 1].y * sn;
+            }
+            y[k] = mk<C>(a.x + b.y, a.y - b.x);
+            y[R - k] = mk<C>(a.x - b.y, a.y + b.x);
+        }
+#pragma unroll
+        for (int r = 0; r < R; r++) v[r] = y[r];
+    }
+};
+template <typename C> struct Dft<C, 11> : DftOdd<C, 11> {};
+template <typename C> struct Dft<C, 13> : DftOdd<C, 13> {};
+template <typename C> struct Dft<C, 17> : DftOdd<C, 17> {};
+template <typename C> struct Dft<C, 19> : DftOdd<C, 19> {};
+template <typename C> struct Dft<C, 23> : DftOdd<C, 23> {};
+
 // ---------------------------------------------------------------- view access
 // Complex element (v, n) of a CView; `conj` negates the imaginary part.
 template <typename T> struct CAcc {
@@ -1235,10 +1385,15 @@ __device__ __forceinline__ void gpass_body(const GPassArgs<T> &a, long v, int j)
     }
 }
 
-// Radices with a codelet; any other radix is an odd prime taken as a direct sum.
+// Radices with a codelet; any other radix is an odd prime, taken by the
+// odd-prime codelet up to 23 (one thread per butterfly, own kernel instance)
+// and as a direct sum above.
 __host__ __device__ __forceinline__ bool gpass_codelet(int R) {
     return R == 2 || R == 3 || R == 4 || R == 5 || R == 6 || R == 7 || R == 8 || R == 9 || R == 10 || R == 12 ||
            R == 14 || R == 15 || R == 16;
+}
+__host__ __device__ __forceinline__ bool gpass_prime(int R) {
+    return R == 11 || R == 13 || R == 17 || R == 19 || R == 23;
 }
 
 // Output k of butterfly j of a prime-radix pass as the direct sum over its R
@@ -1275,7 +1430,21 @@ __device__ __forceinline__ void gpass_generic(const GPassArgs<T> &a, long v, int
 // Work items of one pass: a butterfly (j) for codelet radices, an output
 // (j, k) of a butterfly for direct-sum radices.
 __host__ __device__ __forceinline__ long gpass_items(long nvec, int N, int R) {
-    return gpass_codelet(R) ? nvec * (N / R) : nvec * (long)N;
+    return (gpass_codelet(R) || gpass_prime(R)) ? nvec * (N / R) : nvec * (long)N;
+}
+
+// A pass of an odd prime radix R <= 23: one thread per butterfly, the R
+// inputs loaded once (in a kernel of its own, so the registers of its codelet
+// do not count against the other radices' kernel).
+template <typename T, int R>
+__global__ void __launch_bounds__(256) k_gpass_prime(const GPassArgs<T> pa) {
+    const GPassArgs<T> a = pa;
+    const long NR = a.N / R;
+    const long total = a.nvec * NR;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const long v = i / NR;
+        gpass_body<T, R>(a, v, (int)(i - v * NR));
+    }
 }
 
 template <typename T>

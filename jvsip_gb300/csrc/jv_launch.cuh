@@ -384,7 +384,14 @@ static bool gpass(const GPassArgs<T> &a, cudaStream_t st) {
     long gmax = (long)d->sms * 32;
     if (grid > gmax) grid = gmax;
     if (grid < 1) grid = 1;
-    k_gpass<T><<<(unsigned)grid, 256, 0, st>>>(a);
+    switch (gpass_prime(a.R) ? a.R : 0) {
+        case 11: k_gpass_prime<T, 11><<<(unsigned)grid, 256, 0, st>>>(a); break;
+        case 13: k_gpass_prime<T, 13><<<(unsigned)grid, 256, 0, st>>>(a); break;
+        case 17: k_gpass_prime<T, 17><<<(unsigned)grid, 256, 0, st>>>(a); break;
+        case 19: k_gpass_prime<T, 19><<<(unsigned)grid, 256, 0, st>>>(a); break;
+        case 23: k_gpass_prime<T, 23><<<(unsigned)grid, 256, 0, st>>>(a); break;
+        default: k_gpass<T><<<(unsigned)grid, 256, 0, st>>>(a); break;
+    }
     count_launch();
     return cuda_ok(cudaGetLastError(), "k_gpass launch");
 }
