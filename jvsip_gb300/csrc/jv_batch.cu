@@ -164,51 +164,63 @@ __global__ void __cluster_dims__(kColCluster, 1, 1) __launch_bounds__(BT, 1)
     if (t >= ntiles) return;                 // uniform over the cluster
     if (threadIdx.x == 0) sd = q[t];
     __syncthreads();
-    const int tid = threadIdx.x, nthr = blockDim.x;
-    const int N = sd.N, nt = sd.nt;
-    const int Q = (N + kColCluster - 1) / kColCluster;
-    const int n0 = rank * Q, nr = max(0, min(N, n0 + Q) - n0);
-    const int tot = nr * nt;
-    const unsigned mnt = sd.mnt;
-    const float2 *in = reinterpret_cast<const float2 *>(sd.in) + (sd.in_off + sd.v0 * sd.in_vs);
-    const long ies = sd.in_es, ivs = sd.in_vs;
-    const float sgn = sd.inv ? -1.f : 1.f;
-    // ---- load: (row, column) with the column fastest, four loads in flight
-    for (int i0 = tid; i0 < tot; i0 += 4 * nthr) {
-        float2 c[4];
-        int kk[4], nn[4];
+    // each phase reads its values from the shared descriptor, so none of them
+    // stays live in registers across the passes (which use all 64)
+    {
+        // ---- load: (row, column) with the column fastest, four loads in flight
+        const int tid = threadIdx.x, nthr = blockDim.x;
+        const int N = sd.N, nt = sd.nt;
+        const int Q = (N + kColCluster - 1) / kColCluster;
+        const int n0 = rank * Q, nr = max(0, min(N, n0 + Q) - n0);
+        const int tot = nr * nt;
+        const unsigned mnt = sd.mnt;
+        const float2 *in = reinterpret_cast<const float2 *>(sd.in) + (sd.in_off + sd.v0 * sd.in_vs);
+        const long ies = sd.in_es, ivs = sd.in_vs;
+        const float sgn = sd.inv ? -1.f : 1.f;
+        for (int i0 = tid; i0 < tot; i0 += 4 * nthr) {
+            float2 c[4];
+            int kk[4], nn[4];
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const int i = i0 + u * nthr;
-            kk[u] = 0;
-            nn[u] = 0;
-            if (i < tot) {
-                const int r = mdiv(i, mnt);
-                kk[u] = i - r * nt;
-                nn[u] = n0 + r;
-                c[u] = in[(long)kk[u] * ivs + (long)nn[u] * ies];
+            for (int u = 0; u < 4; u++) {
+                const int i = i0 + u * nthr;
+                kk[u] = 0;
+                nn[u] = 0;
+                if (i < tot) {
+                    const int r = mdiv(i, mnt);
+                    kk[u] = i - r * nt;
+                    nn[u] = n0 + r;
+                    c[u] = in[(long)kk[u] * ivs + (long)nn[u] * ies];
+                }
             }
-        }
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-            if (i0 + u * nthr < tot) {
-                float2 *dst = cl.map_shared_rank(s, kk[u]);
-                dst[nn[u]] = make_float2(c[u].x, c[u].y * sgn);
+            for (int u = 0; u < 4; u++) {
+                if (i0 + u * nthr < tot) {
+                    float2 *dst = cl.map_shared_rank(s, kk[u]);
+                    dst[nn[u]] = make_float2(c[u].x, c[u].y * sgn);
+                }
             }
         }
     }
     cl.sync();
-    if (rank < nt) col_passes(s, sd.ld, sd.passes, sd.twg, sd.pc);
+    if ((int)cl.block_rank() < sd.nt) col_passes(s, sd.ld, sd.passes, sd.twg, sd.pc);
     cl.sync();
-    // ---- store: rows [n0, n0 + nr) of the columns, from their owners
-    float2 *out = reinterpret_cast<float2 *>(sd.out) + (sd.out_off + sd.v0 * sd.out_vs);
-    const long oes = sd.out_es, ovs = sd.out_vs;
-    const float scale = sd.has_scale ? sd.scale : 1.f, sy = sgn * scale;
-    for (int i = tid; i < tot; i += nthr) {
-        const int r = mdiv(i, mnt), k = i - r * nt, n = n0 + r;
-        const float2 *src = cl.map_shared_rank(s, k);
-        const float2 v = src[spad(n)];
-        out[(long)k * ovs + (long)n * oes] = make_float2(v.x * scale, v.y * sy);
+    {
+        // ---- store: rows [n0, n0 + nr) of the columns, from their owners
+        const int tid = threadIdx.x, nthr = blockDim.x;
+        const int N = sd.N, nt = sd.nt;
+        const int Q = (N + kColCluster - 1) / kColCluster;
+        const int n0 = (int)cl.block_rank() * Q, nr = max(0, min(N, n0 + Q) - n0);
+        const int tot = nr * nt;
+        const unsigned mnt = sd.mnt;
+        float2 *out = reinterpret_cast<float2 *>(sd.out) + (sd.out_off + sd.v0 * sd.out_vs);
+        const long oes = sd.out_es, ovs = sd.out_vs;
+        const float scale = sd.has_scale ? sd.scale : 1.f, sy = (sd.inv ? -1.f : 1.f) * scale;
+        for (int i = tid; i < tot; i += nthr) {
+            const int r = mdiv(i, mnt), k = i - r * nt, n = n0 + r;
+            const float2 *src = cl.map_shared_rank(s, k);
+            const float2 v = src[spad(n)];
+            out[(long)k * ovs + (long)n * oes] = make_float2(v.x * scale, v.y * sy);
+        }
     }
     cl.sync();
 }
