@@ -384,13 +384,15 @@ static bool gpass(const GPassArgs<T> &a, cudaStream_t st) {
     long gmax = (long)d->sms * 32;
     if (grid > gmax) grid = gmax;
     if (grid < 1) grid = 1;
-    switch (gpass_prime(a.R) ? a.R : 0) {
-        case 11: k_gpass_prime<T, 11><<<(unsigned)grid, 256, 0, st>>>(a); break;
-        case 13: k_gpass_prime<T, 13><<<(unsigned)grid, 256, 0, st>>>(a); break;
-        case 17: k_gpass_prime<T, 17><<<(unsigned)grid, 256, 0, st>>>(a); break;
-        case 19: k_gpass_prime<T, 19><<<(unsigned)grid, 256, 0, st>>>(a); break;
-        case 23: k_gpass_prime<T, 23><<<(unsigned)grid, 256, 0, st>>>(a); break;
-        default: k_gpass<T><<<(unsigned)grid, 256, 0, st>>>(a); break;
+    const unsigned g = (unsigned)grid;
+    switch (a.R) {
+#define JV_GPASS_R(R) \
+    case R: k_gpass_r<T, R><<<g, 256, 0, st>>>(a); break;
+        JV_GPASS_R(2) JV_GPASS_R(3) JV_GPASS_R(4) JV_GPASS_R(5) JV_GPASS_R(6) JV_GPASS_R(7) JV_GPASS_R(8)
+        JV_GPASS_R(9) JV_GPASS_R(10) JV_GPASS_R(12) JV_GPASS_R(14) JV_GPASS_R(15) JV_GPASS_R(16)
+        JV_GPASS_R(11) JV_GPASS_R(13) JV_GPASS_R(17) JV_GPASS_R(19) JV_GPASS_R(23)
+#undef JV_GPASS_R
+        default: k_gpass<T><<<g, 256, 0, st>>>(a); break;  // primes above 23: direct sums
     }
     count_launch();
     return cuda_ok(cudaGetLastError(), "k_gpass launch");
