@@ -1448,6 +1448,66 @@ __global__ void __launch_bounds__(256) k_gpass_r(const GPassArgs<T> pa) {
     }
 }
 
+// Shared-memory pitch (elements) of a thread's R outputs in the first pass's
+// staging: odd, so a half-warp's 64-bit stores hit distinct banks.
+template <int R> __host__ __device__ constexpr int gpass_stage_pitch() { return R | 1; }
+
+// The first pass (Ns = 1) of a multi-pass transform: butterfly j writes its R
+// outputs to j*R .. j*R + R - 1, so a CTA's 256 consecutive butterflies
+// (i = v*N/R + j over the transforms) fill the contiguous outputs
+// [i0*R, (i0 + 256)*R) of the flattened (v, n) output space.  They go through
+// shared memory (with each slot's transform and butterfly, so the stores need
+// no division) and leave as 256-element coalesced runs instead of R elements
+// 8*R bytes apart per store instruction.  Every thread of the CTA
+// runs the same loop trips (the barriers), with its own butterfly when it has one.
+template <typename T, int R>
+__global__ void __launch_bounds__(256) k_gpass_r1(const GPassArgs<T> pa) {
+    typedef typename cplx_t<T>::t C;
+    extern __shared__ __align__(16) unsigned char gsm_raw[];
+    C *stg = reinterpret_cast<C *>(gsm_raw);
+    __shared__ long bv[256];  // transform and butterfly of each staged slot
+    __shared__ int bj[256];
+    constexpr int P = gpass_stage_pitch<R>();
+    const GPassArgs<T> a = pa;
+    const long NR = a.N / R;
+    const long total = a.nvec * NR;
+    const int t = threadIdx.x;
+    for (long i0 = (long)blockIdx.x * 256; i0 < total; i0 += (long)gridDim.x * 256) {
+        const long i = i0 + t;
+        if (i < total) {
+            const long v = i / NR;
+            const int j = (int)(i - v * NR);
+            bv[t] = v;
+            bj[t] = j;
+            C x[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                C c;
+                if (a.src_real) c = mk<C>(a.rsrc.load(v, 2 * (j + r * NR)), a.rsrc.load(v, 2 * (j + r * NR) + 1));
+                else c = a.src.load(v, j + r * NR);
+                if (a.conj_in) c.y = -c.y;
+                x[r] = c;
+            }
+            Dft<C, R>::run(x);
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                C c = x[r];
+                if (a.conj_out) c.y = -c.y;
+                if (a.has_scale) c = cscale(c, a.scale);
+                stg[t * P + r] = c;
+            }
+        }
+        __syncthreads();
+        const int cnt = (int)(total - i0 < 256 ? total - i0 : 256) * R;  // outputs of this trip
+        for (int e = t; e < cnt; e += 256) {
+            // output r of staged butterfly q: element j*R + r of its transform
+            const int q = e / R, r = e - q * R;
+            a.dst.store(bv[q], (long)bj[q] * R + r, stg[q * P + r]);
+        }
+        __syncthreads();
+    }
+}
+
 // A pass of a prime radix above 23 as direct sums, one thread per output.
 template <typename T>
 __global__ void __launch_bounds__(256) k_gpass(const GPassArgs<T> pa) {

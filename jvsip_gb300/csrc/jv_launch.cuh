@@ -385,9 +385,18 @@ static bool gpass(const GPassArgs<T> &a, cudaStream_t st) {
     if (grid > gmax) grid = gmax;
     if (grid < 1) grid = 1;
     const unsigned g = (unsigned)grid;
+    typedef typename cplx_t<T>::t C;
+    // the first pass (Ns = 1) stages its outputs in shared memory when the
+    // staging and the slots' indices (256 x (8 + 4) bytes of static shared
+    // memory) fit the default 48 KB (coalesced stores)
     switch (a.R) {
-#define JV_GPASS_R(R) \
-    case R: k_gpass_r<T, R><<<g, 256, 0, st>>>(a); break;
+#define JV_GPASS_R(R)                                                                               \
+    case R:                                                                                         \
+        if (a.Ns == 1 && 256 * gpass_stage_pitch<R>() * sizeof(C) + 256 * 12 <= 48 * 1024)          \
+            k_gpass_r1<T, R><<<g, 256, 256 * gpass_stage_pitch<R>() * sizeof(C), st>>>(a);          \
+        else                                                                                        \
+            k_gpass_r<T, R><<<g, 256, 0, st>>>(a);                                                  \
+        break;
         JV_GPASS_R(2) JV_GPASS_R(3) JV_GPASS_R(4) JV_GPASS_R(5) JV_GPASS_R(6) JV_GPASS_R(7) JV_GPASS_R(8)
         JV_GPASS_R(9) JV_GPASS_R(10) JV_GPASS_R(12) JV_GPASS_R(14) JV_GPASS_R(15) JV_GPASS_R(16)
         JV_GPASS_R(11) JV_GPASS_R(13) JV_GPASS_R(17) JV_GPASS_R(19) JV_GPASS_R(23)
