@@ -130,7 +130,7 @@ def test_split_form_unaligned_rows():
 
 @pytest.mark.parametrize("in_off,out_off", [(0, 1), (1, 0)], ids=["out-odd", "in-odd"])
 def test_split_form_mixed_alignment(in_off, out_off):
-    # one side on 16-byte row boundaries (bulk copies), the other 8 bytes off
+    # one side on 16-byte row boundaries, the other 8 bytes off
     Mr = 21
     z = scaled_rows(Mr, 47)
     x = np.zeros(2 * (in_off + Mr * N), np.float32)
