@@ -465,9 +465,8 @@ int jvsip_komega_f(const vsip_fftm_f *rcfftm, const vsip_fftm_f *ccfftm,
 
 /* Complex-to-complex multiple FFT that allocates nothing (no counterpart in
  * the reference).  For callers that cannot allocate device memory when they
- * transform: code running during CUDA stream capture, real-time threads that
- * must not block in the allocator, applications whose device memory is fully
- * reserved up front.  `plan` is a ccfftmop/ccfftmip _f plan made beforehand;
+ * transform: real-time threads that must not block in the allocator,
+ * applications whose device memory is fully reserved up front.  `plan` is a ccfftmop/ccfftmip _f plan made beforehand;
  * x and y are device pointers to interleaved complex float data (equal for an
  * in-place call).  For VSIP_ROW plans the mN transforms are rows of MN
  * contiguous points, x_pitch / y_pitch complex elements apart; for VSIP_COL
@@ -475,8 +474,8 @@ int jvsip_komega_f(const vsip_fftm_f *rcfftm, const vsip_fftm_f *ccfftm,
  * apart.  The intermediate buffers come from a fixed 16 MiB array in device
  * memory that is part of the library (held on every GPU that loads it until
  * exit): mN*MN may not exceed 1048576 complex points, larger calls return an
- * error.  The array's address is looked up on the first call on each device,
- * so make that call before any stream capture.  x and y must be the same buffer
+ * error.  The array's address is looked up once, by the first call.  x and y
+ * must be the same buffer
  * or not overlap.  All calls share the array and
  * it keeps the last call's contents; calls that overlap on the GPU race on it.
  * Work is queued on the library stream (jvsip_gpu_stream); returns 0 when it

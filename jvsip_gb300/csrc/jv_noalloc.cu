@@ -1,11 +1,9 @@
 // jv_noalloc.cu -- a complex-to-complex multiple FFT that allocates nothing.
 //
 // Some callers cannot allocate device memory at the moment they need a
-// transform: code that runs while a CUDA stream is being captured into a
-// graph (cudaMalloc is not allowed during capture, and a stream-ordered
-// allocation would be recorded into the graph), real-time or interrupt-driven
-// threads that must not block in the driver's allocator, and applications
-// whose device memory is reserved in full up front by another framework.
+// transform: real-time or interrupt-driven threads that must not block in the
+// driver's allocator, and applications whose device memory is reserved in
+// full up front by another framework.
 // jvsip_ccfftm_noalloc_f serves them.  It runs the library's multi-pass
 // global-memory transform -- the path used for lengths with prime factors
 // above 7 or lengths too long for shared memory -- with the two intermediate
@@ -18,8 +16,7 @@
 // not exceed it; larger calls are rejected with an error.  The array lives on
 // every GPU that loads the library until the process exits.  Its address on
 // the library's device is looked up once, by the first call (which makes that
-// device current for the lookup); make that first call before any stream
-// capture begins.  Every call uses the
+// device current for the lookup).  Every call uses the
 // same array and it keeps the last call's contents; nothing in it has to start
 // at zero because every pass writes all the scratch it later reads.  Calls are
 // issued on the library's stream, so calls from this library are ordered;

@@ -1,8 +1,8 @@
 """The no-allocation transform (jvsip_ccfftm_noalloc_f) through the C ABI.
 
-Callers that cannot allocate device memory when they transform (code running
-during stream capture, real-time threads, applications whose device memory is
-reserved up front) use this entry point; its intermediate buffers come from a
+Callers that cannot allocate device memory when they transform (real-time
+threads, applications whose device memory is reserved up front) use this entry
+point; its intermediate buffers come from a
 fixed array inside the library.  Its output must match the regular
 vsip_ccfftmop_f entry point on the same plan and data, on two calls in a row,
 within the parity tolerance rel-L2 <= 1e-6*log2(N).  This file is collected
