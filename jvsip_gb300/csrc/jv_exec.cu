@@ -366,11 +366,12 @@ static bool two_steps(const Job &j, LongPlan *lp, const CView &in, const CView &
         b.bvs_out = out.es;
     }
     if (j.prec == P_F32) {
-        // single groups of lengths the register-resident kernel takes as column tiles
-        const bool fa = a.nbatch == 1 && launch_fast_step_f32(a, st);
+        // steps of lengths the register-resident kernel takes as column tiles
+        // (groups along the grid's y)
+        const bool fa = launch_fast_step_f32(a, st);
         if (!fa && jvsip_gpu_last_error()) return false;
         if (!fa && !launch_smem_f32(a, st)) return false;
-        const bool fb = b.nbatch == 1 && launch_fast_step_f32(b, st);
+        const bool fb = launch_fast_step_f32(b, st);
         if (!fb && jvsip_gpu_last_error()) return false;
         return fb || launch_smem_f32(b, st);
     }

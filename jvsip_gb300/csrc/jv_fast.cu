@@ -99,8 +99,12 @@ bool fast_step_len(long N) {
     return N == 64 || N == 128 || N == 256 || N == 512 || N == 1000 || N == 1024 || N == 2048 || N == 4096;
 }
 
+// A step of a long transform as column tiles: single vectors (one group), and
+// the steps of several vectors, a group per grid row (the vectors of a group
+// along the tiles, or the groups' twiddle exponent from the grid row).
 bool launch_fast_step_f32(const Job &j, cudaStream_t st) {
-    if (j.kind != K_C2C || j.prec != P_F32 || j.nbatch != 1 || !fast_step_len(j.N) || !j.twp) return false;
+    if (j.kind != K_C2C || j.prec != P_F32 || j.nbatch < 1 || j.nbatch > 65535 || !fast_step_len(j.N) || !j.twp)
+        return false;
     const int ci = j.conj_in < 0 ? j.inv : j.conj_in, co = j.conj_out < 0 ? j.inv : j.conj_out;
     if (ci != j.inv || co != j.inv) return false;
     const CView &a = j.cin, &b = j.cout;

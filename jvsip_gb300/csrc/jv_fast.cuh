@@ -66,9 +66,13 @@ struct FastArgs {
     const float *in_re, *in_im;
     float *out_re, *out_im;
     // output twiddle of the first step of a long transform (TW instances):
-    // element k of transform g times W^(g*k) = tw_lo[m & tw_mask] * tw_hi[m >> tw_sh]
+    // element k of transform row of group y times W^(g*k), g = row*tw_ts +
+    // y*tw_ys, = tw_lo[m & tw_mask] * tw_hi[m >> tw_sh]
     const float2 *tw_lo, *tw_hi;
-    unsigned tw_mask, tw_sh;
+    unsigned tw_mask, tw_sh, tw_ts, tw_ys;
+    // column tiles (COLS instances): groups of nvec transforms along the
+    // grid's y, bvs_in / bvs_out complex elements apart
+    long bvs_in, bvs_out;
     // one pass of a large-radix Stockham transform of Nt = 2^k points (SP
     // instances; the kernel's N is the pass radix R): transform j reads
     // element n at j + n*Nt/R (es_in), multiplies it by W_Nt^(n*m*Nt/(Ns*R))
@@ -196,6 +200,7 @@ struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>, SPLIT, COLS, TW, SP, RM, FXK
                 // rows (1, 32-bit offsets), column tiles (es_out), Stockham
                 // passes ((row - m)*R + m + k*Ns)
                 long ob = a.off_out + row * a.vs_out;
+                if constexpr (COLS) ob += (long)blockIdx.y * a.bvs_out;
                 long ks = COLS ? a.es_out : 1L;
                 if constexpr (SP) {
                     const unsigned m = (unsigned)row & (a.sp_ns - 1u);
@@ -213,7 +218,8 @@ struct Passes<N, T, E, NsIn, Off, RList<R0, Rs...>, SPLIT, COLS, TW, SP, RM, FXK
                         float2 c = v[b * R0 + r];
                         if constexpr (TW)
                             c = cmul(c, tw_two_level(a.tw_lo, a.tw_hi, a.tw_mask, a.tw_sh,
-                                                     (unsigned)row * (unsigned)(j + r * NsIn)));
+                                                     ((unsigned)row * a.tw_ts + blockIdx.y * a.tw_ys) *
+                                                         (unsigned)(j + r * NsIn)));
                         if (a.inv) c.y = -c.y;
                         if (a.has_scale) c = cscale(c, a.scale);
                         const int k = j + r * NsIn;
@@ -289,7 +295,7 @@ __global__ void __launch_bounds__(T *RPC, fast_min_blocks<N, T, RPC, SP>()) k_fa
     const long rowc = live ? row : a.nvec - 1;
     float2 v[E];
     // base pointers of the transform; rows index them with 32-bit offsets
-    const long ib = a.off_in + rowc * a.vs_in;
+    const long ib = a.off_in + rowc * a.vs_in + (COLS ? (long)blockIdx.y * a.bvs_in : 0L);
     const float2 *inb = a.in + ib;
     const float *inr = a.in_re + ib, *ini = a.in_im + ib;
     constexpr int B1 = E / R1;
@@ -365,6 +371,10 @@ static bool launch_fast_n(const Job &j, cudaStream_t st) {
     a.tw_hi = (const float2 *)j.tw_hi;
     a.tw_mask = j.tw_mask;
     a.tw_sh = j.tw_sh;
+    a.tw_ts = j.tw_ts;
+    a.tw_ys = j.tw_ys;
+    a.bvs_in = j.bvs_in;
+    a.bvs_out = j.bvs_out;
     a.in = (const float2 *)j.cin.re;
     a.out = (float2 *)j.cout.re;
     a.es_in = j.cin.es;
@@ -422,7 +432,10 @@ static bool launch_fast_n(const Job &j, cudaStream_t st) {
         attr = true;
     }
     long grid = (j.nvec + RPC - 1) / RPC;
-    k_fast<N, T, RPC, L, SPLIT, COLS, TW, SP, RM, FXK><<<(unsigned)grid, T * RPC, smem, st>>>(a);
+    // groups along y: column-tile steps of a long transform (at most 65535)
+    const unsigned gy = COLS ? (unsigned)j.nbatch : 1u;
+    if (gy < 1 || gy > 65535u) return false;
+    k_fast<N, T, RPC, L, SPLIT, COLS, TW, SP, RM, FXK><<<dim3((unsigned)grid, gy), T * RPC, smem, st>>>(a);
     count_launch();
     return cuda_ok(cudaGetLastError(), "k_fast launch");
 }
