@@ -226,9 +226,22 @@ __global__ void __cluster_dims__(kColCluster, 1, 1) __launch_bounds__(BT, 1)
 }
 
 // ---------------------------------------------------------------- host side
+// A call the batch runs through the plain path instead of tiles: single-
+// precision c2c columns (adjacent vectors on both sides) of 8192 points or
+// more, which the plain calls take as two steps (on the register-resident
+// column tiles or the shared-memory kernel, the groups along the grid's y).
+// Measured on the 2 GB batch: its columns of 8192-16384 points 1.052 ms this
+// way against 1.185 ms on the column clusters; columns of 3000-8191 points
+// were slower this way than as tiles (0.94 against 0.72 ms).
+struct StepCall {
+    Plan *p;
+    const vsip_cmview_f *x, *y;
+};
+
 struct BatchBuild {
     std::vector<TileDesc> tiles[kClasses];
     size_t smem[kClasses] = {0, 0, 0, 0};
+    std::vector<StepCall> steps;
     double bytes = 0;
 };
 
@@ -321,6 +334,11 @@ static bool build_tiles(size_t n, const vsip_fftm_f *const plans[], const vsip_c
         bool vf_out = labs(t.out_vs) == 1 && labs(t.out_es) != 1;
         t.vec_fast = (vf_in || vf_out) ? 1 : 0;
         t.ld = (int)tile_ld(N, t.vec_fast);
+        if (N >= kLongFewMin && resident_long_columns_f(p, x, y)) {
+            bb.steps.push_back(StepCall{p, x, y});
+            bb.bytes += 16.0 * N * nv;
+            continue;
+        }
         if (t.vec_fast && 2 * N > BEMAX * BT) {
             // columns of long transforms: groups of up to kColCluster adjacent
             // columns, one cluster each (k_batch_cols)
@@ -378,9 +396,15 @@ struct DevBatch {
     int n[kClasses] = {0, 0, 0, 0};    // descriptors of each class
     size_t smem[kClasses] = {0, 0, 0, 0};
     int total = 0;
+    std::vector<StepCall> steps;      // calls run through the plain path
 };
 
 static bool upload(const BatchBuild &bb, DevBatch &db) {
+    // the step calls' plans get their scratch now (nothing may allocate while
+    // a batch is recorded into its graph)
+    db.steps = bb.steps;
+    for (const StepCall &c : db.steps)
+        if (!enqueue_resident_c2c_f(c.p, c.x, c.y, nullptr, true)) return false;
     std::vector<TileDesc> all;
     for (int c = 0; c < kClasses; c++) {
         db.off[c] = (int)all.size();
@@ -449,9 +473,10 @@ static bool launch_one(const DevBatch &db, int c, cudaStream_t st) {
 
 // Streams and events the classes run on side by side (forked from and joined
 // back to the caller's stream; the same pattern is recorded into the graph).
+constexpr int kStepStreams = 4;  // streams of the calls run through the plain path
 struct BatchStreams {
-    cudaStream_t s[kClasses] = {nullptr, nullptr, nullptr, nullptr};
-    cudaEvent_t fork = nullptr, join[kClasses] = {nullptr, nullptr, nullptr, nullptr};
+    cudaStream_t s[kClasses + kStepStreams] = {};  // the classes', then the plain-path calls'
+    cudaEvent_t fork = nullptr, join[kClasses + kStepStreams] = {};
     bool ready = false;
 };
 static BatchStreams g_bs;
@@ -461,24 +486,42 @@ static bool batch_streams() {
     std::lock_guard<std::mutex> lk(g_bs_mu);
     if (g_bs.ready) return true;
     bool ok = cuda_ok(cudaEventCreateWithFlags(&g_bs.fork, cudaEventDisableTiming), "batch event");
-    for (int c = 0; c < kClasses && ok; c++)
+    for (int c = 0; c < kClasses + kStepStreams && ok; c++)
         ok = cuda_ok(cudaStreamCreateWithFlags(&g_bs.s[c], cudaStreamNonBlocking), "batch stream") &&
              cuda_ok(cudaEventCreateWithFlags(&g_bs.join[c], cudaEventDisableTiming), "batch event");
     g_bs.ready = ok;
     return ok;
 }
 
+// the plain-path calls on their streams; calls of one plan share its scratch,
+// so they all go to one stream, in order
+static int step_stream(const StepCall &c) { return (int)(((uintptr_t)c.p >> 6) % kStepStreams); }
+
 static bool launch(const DevBatch &db, cudaStream_t st) {
-    if (db.total == 0) return true;
+    if (db.total == 0 && db.steps.empty()) return true;
     int used = 0, only = 0;
     for (int c = 0; c < kClasses; c++)
         if (db.n[c]) {
             used++;
             only = c;
         }
-    if (used == 1) return launch_one(db, only, st);
+    if (used == 1 && db.steps.empty()) return launch_one(db, only, st);
     if (!batch_streams()) return false;
     bool ok = cuda_ok(cudaEventRecord(g_bs.fork, st), "batch fork");
+    if (!db.steps.empty()) {
+        bool on[kStepStreams] = {};
+        for (const StepCall &c : db.steps) {
+            const int k = step_stream(c);
+            cudaStream_t sl = g_bs.s[kClasses + k];
+            if (!on[k]) ok = ok && cuda_ok(cudaStreamWaitEvent(sl, g_bs.fork, 0), "batch fork");
+            on[k] = true;
+            ok = ok && enqueue_resident_c2c_f(c.p, c.x, c.y, sl, false);
+        }
+        for (int k = 0; k < kStepStreams && ok; k++)
+            if (on[k])
+                ok = cuda_ok(cudaEventRecord(g_bs.join[kClasses + k], g_bs.s[kClasses + k]), "batch join") &&
+                     cuda_ok(cudaStreamWaitEvent(st, g_bs.join[kClasses + k], 0), "batch join");
+    }
     // largest CTAs first: they hold the longest tiles
     for (int c = kClasses - 1; c >= 0 && ok; c--) {
         if (!db.n[c]) continue;
@@ -583,7 +626,7 @@ int jvsip_fftm_batch_run_f(jvsip_fftm_batchplan_f *b) {
     if (!b) return E_ARG;
     Device *d = device();
     if (!d) return E_NODEVICE;
-    if (b->db.total == 0) return 0;
+    if (b->db.total == 0 && b->db.steps.empty()) return 0;
     if (!cuda_ok(cudaGraphLaunch(b->exec, d->stream), "batch graph launch")) return E_CUDA;
     count_launch();
     for (const void *blk : b->blocks) {

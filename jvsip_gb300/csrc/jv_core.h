@@ -253,6 +253,13 @@ struct Plan {
 
 Plan *plan_of(const void *vsip_plan);   // ext_fftm_obj of a vsip_fftm_* (nullptr if bad)
 Plan *plan_of_v(const void *vsip_plan); // ext_fft_obj of a vsip_fft_* (nullptr if bad)
+// A single-precision c2c call on views of admitted interleaved blocks, enqueued
+// on `st` with no host synchronisation (the batching form's route for long
+// columns); with `prepare` only the plan's long-transform scratch is made
+// ready and nothing is launched.  False (error set) when it cannot run so.
+bool enqueue_resident_c2c_f(Plan *p, const vsip_cmview_f *x, const vsip_cmview_f *y, cudaStream_t st, bool prepare);
+// true when such a call of plan p on these views runs as the long columns' two steps
+bool resident_long_columns_f(Plan *p, const vsip_cmview_f *x, const vsip_cmview_f *y);
 
 // factorisation of the reference (c_VSIP_src/VI_nuV.h:22-136); returns the stage count
 unsigned long ref_factor(unsigned long N, unsigned long *pn, unsigned long *p0, unsigned long *pF);

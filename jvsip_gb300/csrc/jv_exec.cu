@@ -857,6 +857,45 @@ static void exec_cc(Plan *p, const CMV *x, const CMV *y, bool ip) {
     if (ok) mark_written(same_view ? (const void *)x->block : (const void *)y->block);
 }
 
+// The job of a c2c call of plan p on views of admitted interleaved blocks
+// (both resident), or false.
+static bool resident_job_f(Plan *p, const vsip_cmview_f *x, const vsip_cmview_f *y, Job &j) {
+    if (!p || p->prec != P_F32 || (p->type != JV_CCFFTOP && p->type != JV_CCFFTIP) || !x || !y || !x->block ||
+        !y->block)
+        return false;
+    if (!view_ok(x, p->major, p->MN, p->mN) || !view_ok(y, p->major, p->MN, p->mN)) return false;
+    CRes<float, vsip_cblock_f> rx{x->block, cgeo(x, p->major, p->MN, p->mN), mirror_find(x->block)};
+    CRes<float, vsip_cblock_f> ry{y->block, cgeo(y, p->major, p->MN, p->mN), mirror_find(y->block)};
+    if (!rx.m || !ry.m) return false;
+    const bool same = (x->block == y->block && rx.g.off == ry.g.off && rx.g.es == ry.g.es && rx.g.vs == ry.g.vs);
+    if (x->block == y->block && !same) return false;
+    fill_job(j, p, K_C2C);
+    Staging stg;  // stays empty: both views are resident
+    j.cin = dev_c(stg, rx);
+    j.cout = same ? j.cin : dev_c(stg, ry);
+    j.inplace = same ? 1 : 0;
+    return true;
+}
+
+bool resident_long_columns_f(Plan *p, const vsip_cmview_f *x, const vsip_cmview_f *y) {
+    if (!p) return false;
+    std::lock_guard<std::mutex> lk(p->mu);
+    Job j;
+    return resident_job_f(p, x, y, j) && long_columns(j);
+}
+
+bool enqueue_resident_c2c_f(Plan *p, const vsip_cmview_f *x, const vsip_cmview_f *y, cudaStream_t st, bool prepare) {
+    if (!p || !device()) return false;
+    std::lock_guard<std::mutex> lk(p->mu);
+    Job j;
+    if (!resident_job_f(p, x, y, j)) {
+        set_error(E_ARG, "resident c2c call: views of admitted interleaved blocks expected");
+        return false;
+    }
+    if (prepare) return !j.lp || long_scratch(j.lp, long_scratch_need(j), false);
+    return run_job(j, st);
+}
+
 template <typename T, typename RMV, typename CMV, typename RB, typename CB>
 static void exec_rc(Plan *p, const RMV *x, const CMV *z) {
     if (!p || p->type != JV_RCFFTOP) {

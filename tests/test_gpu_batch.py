@@ -142,3 +142,48 @@ def test_autotune_cache(tmp_path, monkeypatch):
     assert L.jvsip_fftm_batch_f(len(seq), P, VI, VO) == 0
     by.sync()
     oracle_check(seq, x, y, offs)
+
+
+def test_batch_long_columns_through_the_plain_two_steps():
+    """Columns of 8192+ points (adjacent, more than one) run through the plain
+    calls' two steps on streams of their own beside the tile launches (one
+    plan's calls on one stream); a single long column keeps the cluster kernel,
+    shorter columns the tiles.  Direct and captured (replayed twice), in place,
+    against the FP64 oracle."""
+    L = J.lib()
+    seq = [(16384, 40, -1, 1), (10000, 7, 1, 1), (8192, 100, 1, 1), (12288, 1, -1, 1), (1000, 30, -1, 0),
+           (3125, 30, -1, 1), (64, 50, 1, 1), (4096, 20, 1, 1)]
+    x, y, bx, by, plans, vin, vout, offs, (P, VI, VO) = make_batch(seq, seed=12)
+    assert L.jvsip_fftm_batch_f(len(seq), P, VI, VO) == 0, J.last_error()
+    by.sync()
+    oracle_check(seq, x, y, offs)
+    direct = y.copy()
+    y[:] = 0
+    by.admit(True)   # re-upload zeros so the replay is what fills the output
+    bp = L.jvsip_fftm_batch_create_f(len(seq), P, VI, VO)
+    assert bp, J.last_error()
+    for _ in range(2):
+        assert L.jvsip_fftm_batch_run_f(bp) == 0
+    by.sync()
+    assert np.array_equal(y, direct)
+    assert L.jvsip_fftm_batch_destroy_f(bp) == 0
+    # in place: x and y the same view
+    x2, _, bx2, _, plans2, vin2, _, offs2, (P2, VI2, _) = make_batch(seq, seed=13)
+    x0 = x2.copy()
+    assert L.jvsip_fftm_batch_f(len(seq), P2, VI2, VI2) == 0, J.last_error()
+    bx2.sync()
+    oracle_check(seq, x0, x2, offs2)
+    # only long columns on the plain path: two plans on the plain-path streams, direct and captured
+    seq3 = [(16384, 12, -1, 1), (8192, 9, 1, 1)]
+    x3, y3, bx3, by3, plans3, vin3, vout3, offs3, (P3, VI3, VO3) = make_batch(seq3, seed=14)
+    assert L.jvsip_fftm_batch_f(len(seq3), P3, VI3, VO3) == 0, J.last_error()
+    by3.sync()
+    oracle_check(seq3, x3, y3, offs3)
+    bp3 = L.jvsip_fftm_batch_create_f(len(seq3), P3, VI3, VO3)
+    assert bp3, J.last_error()
+    y3[:] = 0
+    by3.admit(True)
+    assert L.jvsip_fftm_batch_run_f(bp3) == 0
+    by3.sync()
+    oracle_check(seq3, x3, y3, offs3)
+    assert L.jvsip_fftm_batch_destroy_f(bp3) == 0
