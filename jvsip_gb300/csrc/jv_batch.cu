@@ -12,8 +12,10 @@
 // run side by side on forked streams.  Each CTA first asks L2 for the input
 // of the descriptor one resident wave further down its queue (the CTA that
 // will take this SM slot later), so later tiles' DRAM reads overlap earlier
-// tiles' passes.  A captured batch (jvsip_fftm_batch_create_f) records the
-// launches in a CUDA graph once; jvsip_fftm_batch_run_f replays it.
+// tiles' passes.  Columns of 8192 points or more (adjacent, more than one) go
+// through the plain calls' two steps instead, on four more streams.  A
+// captured batch (jvsip_fftm_batch_create_f) records the launches in a CUDA
+// graph once; jvsip_fftm_batch_run_f replays it.
 //
 // No reference counterpart: VSIPL has no multi-plan call; the reference can
 // only loop plan by plan (c_VSIP_src/VI_ccfftmop_f_def.h:20-29 per call).
