@@ -493,10 +493,11 @@ static bool long_few(const Job &j) {
 // single-precision c2c columns (adjacent vectors on both sides) of a length
 // with a decomposition from kColStepsMin points, not taken by the
 // register-resident column tiles: two steps whatever their count.  Measured
-// against the shared-memory kernel's column tiles: 16384 x 1024: 1799 against
-// 1013 GB/s; 10000 x 1024: 1848 against 917; 8192 x 2048: 1806 against 1436;
-// 7000 x 512: 1319 against 782; 3000 x 1024: 1164 against 874 (and slower than
-// the register-resident tiles: 4096 x 1024: 1457 against 2283).
+// against the shared-memory kernel's column tiles: 16384 x 1024: 3001 against
+// 1013 GB/s (1799 before the steps ran on the register-resident column tiles);
+// 10000 x 1024: 1840 against 917; 8192 x 2048: 2980 against 1436; 7000 x 512:
+// 1319 against 782; 3000 x 1024: 1164 against 874 (and slower than the
+// register-resident tiles themselves: 4096 x 1024: 1457 against 2283).
 static bool long_columns(const Job &j) {
     return j.lp && j.kind == K_C2C && j.prec == P_F32 && j.nvec > 1 && j.N >= kColStepsMin && !fast_step_len(j.N) &&
            labs(j.cin.vs) == 1 && labs(j.cout.vs) == 1;
