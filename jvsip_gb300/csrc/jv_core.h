@@ -175,7 +175,7 @@ constexpr long kLongFewMin = 8192;
 // two steps whatever their count, unless the register-resident column tiles
 // take the length (fast_step_len: powers of two up to 4096 and 1000).
 // Measured on columns of 3000-7776 points (128-1024 of them): 1.1-1.7x the
-// shared-memory kernel's column tiles; 8192-16384 points: 1.0-2.0x; below,
+// shared-memory kernel's column tiles; 8192-16384 points: 1.1-3.0x; below,
 // mixed (2187 x 1024: 1.07x, 2560 x 1024: 0.91x, 2400 x 512: 0.70x).
 constexpr long kColStepsMin = 3000;
 
